@@ -1,0 +1,349 @@
+// grid.cu — uniform-grid hash and deterministic counting sort (arrange stage,
+// rows A2-A5 of the hot path).
+//
+// Reference behaviour (KemengHuang/Fast-General-GPU-SPH-framework):
+//   micro key      src/core/sph_utils.cuh:44-99  (ParticlePos2CellPosM,
+//                  CellPos2CellIdxM): key = (cell << 6) | (mx << 4) | (mz << 2) | my
+//   count          src/grid/sph_arrangement.cu:1331-1341 (CountingSort_Cell_SumM)
+//   offsets        src/grid/sph_arrangement.cu:1370-1371 (CUB ExclusiveSum over
+//                  a dense numc*64+1 micro table)
+//   reorder        src/grid/sph_arrangement.cu:1309-1330 (CountingSort_Result_M)
+//   cell info      src/grid/sph_arrangement.cu:1342-1351 (calculate_cell_info)
+//
+// Design here (not a translation):
+//   * counting is per COARSE cell (numc ints, not numc*64), with warp-aggregated
+//     atomics (match.any) so a warp of sorted particles issues one atomic per
+//     cell it touches;
+//   * the coarse scan is reduce-then-scan (no inter-CTA spin waits) and also
+//     compacts the occupied cells and the list of large cells;
+//   * the order inside a coarse cell is canonical: (micro key, previous index).
+//     The reference's atomic slot order varies run to run; this one does not,
+//     so two runs (and the CPU restatement) give the same permutation;
+//   * per cell, the three micro-x slab boundaries are kept (10 bits each) in
+//     place of the dense micro table; stale entries of empty cells are harmless
+//     because every use clamps them by the cell's count.
+#include "gsph_internal.h"
+
+namespace gsph {
+
+namespace {
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Micro key of one position (sph_utils.cuh:44-99). Positions outside the grid
+// raise kErrOutOfDomain and are clamped to the nearest cell so that no index
+// ever leaves the tables.
+__device__ __forceinline__ uint32_t micro_key(float4 p, const DevParams &P,
+                                              Counters *ctr, int i) {
+    const float fx = floorf(p.x * P.rat);
+    const float fy = floorf(p.y * P.rat);
+    const float fz = floorf(p.z * P.rat);
+    const float lx = float(P.gx << 2), ly = float(P.gy << 2),
+                lz = float(P.gz << 2);
+    int mx, my, mz;
+    if (fx >= 0.f && fx < lx && fy >= 0.f && fy < ly && fz >= 0.f && fz < lz) {
+        mx = int(fx);
+        my = int(fy);
+        mz = int(fz);
+    } else {
+        mx = (fx >= 0.f) ? min(int(fminf(fx, lx - 1.f)), (P.gx << 2) - 1) : 0;
+        my = (fy >= 0.f) ? min(int(fminf(fy, ly - 1.f)), (P.gy << 2) - 1) : 0;
+        mz = (fz >= 0.f) ? min(int(fminf(fz, lz - 1.f)), (P.gz << 2) - 1) : 0;
+        if (atomicOr(&ctr->err, kErrOutOfDomain) == 0u) ctr->err_index = i;
+    }
+    const uint32_t c = uint32_t(mx >> 2) +
+                       uint32_t(P.gx) * (uint32_t(my >> 2) + uint32_t(P.gy) * uint32_t(mz >> 2));
+    const uint32_t sub = uint32_t(my & 3) | (uint32_t(mz & 3) << 2) | (uint32_t(mx & 3) << 4);
+    return (c << 6) | sub;
+}
+
+// ---------------------------------------------------------------------------
+// A2: key + per-coarse-cell slot (warp-aggregated atomics).
+__global__ void __launch_bounds__(256)
+k_hash_count(const float4 *__restrict__ pos, int n, DevParams P,
+             uint32_t *__restrict__ key_out, uint32_t *__restrict__ slot_out,
+             int32_t *__restrict__ cell_count, Counters *ctr) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < n;
+    const unsigned active = __ballot_sync(kFull, valid);
+    if (!valid) return;
+    const uint32_t key = micro_key(pos[i], P, ctr, i);
+    const uint32_t cell = key >> 6;
+    const unsigned peers = __match_any_sync(active, cell);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&cell_count[cell], __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    key_out[i] = key;
+    slot_out[i] = uint32_t(base + __popc(peers & lanemask_lt()));
+}
+
+// ---------------------------------------------------------------------------
+// A3/A5: reduce-then-scan over the coarse counts. Values are packed
+// (occupied << 32) | count so one scan yields the cell offsets and the
+// occupied-cell compaction.
+__device__ __forceinline__ unsigned long long pack_cell(int cnt) {
+    return (cnt > 0 ? (1ull << 32) : 0ull) | (unsigned long long)(unsigned)cnt;
+}
+
+__device__ __forceinline__ void load_tile_counts(const int32_t *__restrict__ in,
+                                                 int n, int first,
+                                                 int (&v)[kScanItems]) {
+    if (first + kScanItems <= n) {
+        const int4 *p4 = reinterpret_cast<const int4 *>(in + first);
+#pragma unroll
+        for (int q = 0; q < kScanItems / 4; ++q) {
+            int4 t = p4[q];
+            v[4 * q + 0] = t.x;
+            v[4 * q + 1] = t.y;
+            v[4 * q + 2] = t.z;
+            v[4 * q + 3] = t.w;
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < kScanItems; ++q)
+            v[q] = (first + q < n) ? in[first + q] : 0;
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+k_cell_scan_reduce(const int32_t *__restrict__ count, int numc,
+                   unsigned long long *__restrict__ tiles) {
+    const int first = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    int v[kScanItems];
+    load_tile_counts(count, numc, first, v);
+    unsigned long long s = 0;
+#pragma unroll
+    for (int q = 0; q < kScanItems; ++q) s += pack_cell(v[q]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(kFull, s, o);
+    __shared__ unsigned long long ws[kScanThreads / 32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+        for (int w = 0; w < kScanThreads / 32; ++w) t += ws[w];
+        tiles[blockIdx.x] = t;
+    }
+}
+
+// Exclusive scan of the tile sums by one CTA; writes the grand total.
+__global__ void __launch_bounds__(1024)
+k_cell_scan_tiles(unsigned long long *__restrict__ tiles, int ntiles,
+                  int32_t *__restrict__ cell_start, int numc, Counters *ctr) {
+    __shared__ unsigned long long ws[32];
+    __shared__ unsigned long long carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int base = 0; base < ntiles; base += blockDim.x) {
+        const int t = base + threadIdx.x;
+        const unsigned long long v = t < ntiles ? tiles[t] : 0ull;
+        unsigned long long x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned long long y = __shfl_up_sync(kFull, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) ws[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            unsigned long long w = ws[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                unsigned long long y = __shfl_up_sync(kFull, w, o);
+                if (lane >= o) w += y;
+            }
+            ws[lane] = w;
+        }
+        __syncthreads();
+        const unsigned long long wprefix = warp > 0 ? ws[warp - 1] : 0ull;
+        const unsigned long long excl = carry + wprefix + x - v;
+        if (t < ntiles) tiles[t] = excl;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        cell_start[numc] = int32_t(carry & 0xFFFFFFFFull);
+        ctr->num_occ = int32_t(carry >> 32);
+        ctr->num_big = 0;
+        ctr->work_density = 0;
+        ctr->work_force = 0;
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+k_cell_scan_apply(const int32_t *__restrict__ count, int numc,
+                  const unsigned long long *__restrict__ tiles,
+                  int32_t *__restrict__ cell_start,
+                  int32_t *__restrict__ occ_list,
+                  int32_t *__restrict__ big_list, Counters *ctr) {
+    const int first = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    int v[kScanItems];
+    load_tile_counts(count, numc, first, v);
+    unsigned long long s = 0;
+#pragma unroll
+    for (int q = 0; q < kScanItems; ++q) s += pack_cell(v[q]);
+    // block exclusive scan of per-thread sums
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long x = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long y = __shfl_up_sync(kFull, x, o);
+        if (lane >= o) x += y;
+    }
+    __shared__ unsigned long long ws[kScanThreads / 32];
+    if (lane == 31) ws[warp] = x;
+    __syncthreads();
+    unsigned long long wprefix = 0;
+    for (int w = 0; w < warp; ++w) wprefix += ws[w];
+    unsigned long long run = tiles[blockIdx.x] + wprefix + x - s;
+#pragma unroll
+    for (int q = 0; q < kScanItems; ++q) {
+        const int c = first + q;
+        if (c < numc) {
+            cell_start[c] = int32_t(run & 0xFFFFFFFFull);
+            if (v[q] > 0) {
+                occ_list[run >> 32] = c;
+                if (v[q] > kSmallCellMax)
+                    big_list[atomicAdd(&ctr->num_big, 1)] = c;
+            }
+        }
+        run += pack_cell(v[q]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Scatter (key, source) pairs to their coarse-cell range (slot order).
+__global__ void __launch_bounds__(256)
+k_scatter_pairs(const uint32_t *__restrict__ key_in,
+                const uint32_t *__restrict__ slot, int n,
+                const int32_t *__restrict__ cell_start,
+                unsigned long long *__restrict__ pairs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t key = key_in[i];
+    const int dst = cell_start[key >> 6] + int(slot[i]);
+    pairs[dst] = ((unsigned long long)key << 32) | (unsigned)i;
+}
+
+__device__ __forceinline__ uint32_t pack_xslab(int s1, int s2, int s3, int cnt) {
+    if (cnt > 1023) return kXslabUnknown;
+    return uint32_t(s1) | (uint32_t(s2) << 10) | (uint32_t(s3) << 20);
+}
+
+__device__ __forceinline__ void move_particle(const Frame &f, int dst,
+                                              unsigned long long e) {
+    const int src = int(e & 0xFFFFFFFFull);
+    f.key[dst] = uint32_t(e >> 32);
+    f.perm[dst] = src;
+    f.pos[dst] = f.pos_in[src];
+    f.vel[dst] = f.vel_in[src];
+    f.ev[dst] = f.ev_in[src];
+}
+
+// Cells with at most kSmallCellMax particles: one thread per particle ranks
+// its pair among the cell's pairs (all distinct: sources are unique).
+__global__ void __launch_bounds__(256) k_sort_small(Frame f) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= f.n) return;
+    const unsigned long long e = f.pairs[s];
+    const uint32_t cell = uint32_t(e >> 38);
+    const int b = f.cell_start[cell];
+    const int cnt = f.cell_start[cell + 1] - b;
+    if (cnt > kSmallCellMax) return;
+    int rank = 0;
+    for (int j = 0; j < cnt; ++j) rank += (f.pairs[b + j] < e) ? 1 : 0;
+    move_particle(f, b + rank, e);
+    if (rank == 0) {
+        int s1 = 0, s2 = 0, s3 = 0;
+        for (int j = 0; j < cnt; ++j) {
+            const int x = int((f.pairs[b + j] >> 36) & 3ull);
+            s1 += x < 1;
+            s2 += x < 2;
+            s3 += x < 3;
+        }
+        f.cell_xslab[cell] = pack_xslab(s1, s2, s3, cnt);
+        f.cell_count[cell] = 0;   // ready for the next frame's atomics
+    }
+}
+
+// Cells with more than kSmallCellMax particles: one CTA per cell, pairs staged
+// in shared memory (global memory beyond kBigCellSmem), rank by counting.
+__global__ void __launch_bounds__(256) k_sort_big(Frame f) {
+    __shared__ unsigned long long sp[kBigCellSmem];
+    __shared__ int slab[3];
+    const int nbig = f.ctr->num_big;
+    for (int q = blockIdx.x; q < nbig; q += gridDim.x) {
+        const int cell = f.big_list[q];
+        const int b = f.cell_start[cell];
+        const int cnt = f.cell_start[cell + 1] - b;
+        const bool in_smem = cnt <= kBigCellSmem;
+        if (threadIdx.x < 3) slab[threadIdx.x] = 0;
+        if (in_smem)
+            for (int j = threadIdx.x; j < cnt; j += blockDim.x) sp[j] = f.pairs[b + j];
+        __syncthreads();
+        const unsigned long long *src = in_smem ? sp : f.pairs + b;
+        int c1 = 0, c2 = 0, c3 = 0;
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+            const unsigned long long e = src[i];
+            int rank = 0;
+            for (int j = 0; j < cnt; ++j) rank += (src[j] < e) ? 1 : 0;
+            move_particle(f, b + rank, e);
+            const int x = int((e >> 36) & 3ull);
+            c1 += x < 1;
+            c2 += x < 2;
+            c3 += x < 3;
+        }
+        atomicAdd(&slab[0], c1);
+        atomicAdd(&slab[1], c2);
+        atomicAdd(&slab[2], c3);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            f.cell_xslab[cell] = pack_xslab(slab[0], slab[1], slab[2], cnt);
+            f.cell_count[cell] = 0;
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+void launch_hash_count(const Frame &f, const DevParams &P, cudaStream_t s) {
+    if (f.n <= 0) return;
+    k_hash_count<<<(f.n + 255) / 256, 256, 0, s>>>(f.pos_in, f.n, P, f.key_in,
+                                                  f.slot, f.cell_count, f.ctr);
+}
+
+void launch_cell_scan(const Frame &f, const DevParams &P, cudaStream_t s) {
+    const int ntiles = (P.numc + kScanTile - 1) / kScanTile;
+    k_cell_scan_reduce<<<ntiles, kScanThreads, 0, s>>>(f.cell_count, P.numc,
+                                                       f.scan_tiles);
+    k_cell_scan_tiles<<<1, 1024, 0, s>>>(f.scan_tiles, ntiles, f.cell_start,
+                                        P.numc, f.ctr);
+    k_cell_scan_apply<<<ntiles, kScanThreads, 0, s>>>(
+        f.cell_count, P.numc, f.scan_tiles, f.cell_start, f.occ_list,
+        f.big_list, f.ctr);
+}
+
+void launch_scatter_pairs(const Frame &f, cudaStream_t s) {
+    if (f.n <= 0) return;
+    k_scatter_pairs<<<(f.n + 255) / 256, 256, 0, s>>>(f.key_in, f.slot, f.n,
+                                                     f.cell_start, f.pairs);
+}
+
+void launch_cell_sort(const Frame &f, int num_sms, cudaStream_t s) {
+    if (f.n <= 0) return;
+    k_sort_small<<<(f.n + 255) / 256, 256, 0, s>>>(f);
+    k_sort_big<<<num_sms * 2, 256, 0, s>>>(f);
+}
+
+}  // namespace gsph

@@ -1,0 +1,114 @@
+// gsph_internal.h — types shared by the host runtime and the device kernels.
+//
+// Layout of one scene in HBM (structure of arrays, 16-byte particle records):
+//   pos[2]  float4[N]  x,y,z, w = 1/rho (ping-pong: the grid sort writes the
+//                      sorted copy into the other buffer)
+//   vel[2]  float4[N]  velocity (w unused; float4 keeps every access 16 B)
+//   ev[2]   float4[N]  evaluated velocity, w = pressure
+//   acc     float4[N]  pressure+viscosity+surface force ("acceleration")
+//   key     uint32[N]  micro-cell key of the sorted particles
+//   cell_start int32[numc+1], cell_xslab uint32[numc]
+#ifndef GSPH_INTERNAL_H_
+#define GSPH_INTERNAL_H_
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/gsph.h"
+
+namespace gsph {
+
+// Cells with more particles than this are ordered by the block-level sort.
+constexpr int kSmallCellMax = 32;
+// Largest cell the block-level sort keeps in shared memory.
+constexpr int kBigCellSmem = 4096;
+// SMS task width (reference sph_utils.cuh:35).
+constexpr int kSmsTaskParticles = 32;
+// Sentinel for cell_xslab: slab boundaries unknown, search the whole cell.
+constexpr uint32_t kXslabUnknown = 0xFFFFFFFFu;
+// Scan tile (items per CTA) for the reduce-then-scan kernels.
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+// Error bits raised by kernels into Counters::err.
+enum : uint32_t {
+    kErrOutOfDomain = 1u,     // a particle's micro cell was outside the grid
+    kErrTaskCapacity = 2u,    // more SMS tasks than the task buffer holds
+};
+
+// Parameters as the kernels see them (passed by value: one constant bank per
+// launch, so several scenes/handles can coexist in one process).
+struct DevParams {
+    float h, h2, rat;            // rat = 4 * inv_cell_size (micro cells)
+    int gx, gy, gz, numc;
+    float density_scale, self_density, rest_density, inv_rest_density;
+    float gas_constant;
+    float half_spiky, visco_coef, grad_color_scale, lplc_color_scale;
+    float surface_normal, surface_coe, mass;
+    float time_step, wall_damping, wall_kernel;   // wall_kernel = h + 0.01
+    float gx_acc, gy_acc, gz_acc;                 // gravity
+    float bmin_x, bmin_y, bmin_z, bmax_x, bmax_y, bmax_z;
+};
+
+// Device-resident counters of one frame (one 128-byte line).
+struct Counters {
+    int32_t num_occ;        // occupied cells
+    int32_t num_big;        // cells sorted by the block-level path
+    int32_t task_count;     // SMS tasks (T)
+    int32_t middle;         // TRA particles
+    int32_t n_sms;          // SMS particles
+    int32_t work_density;   // dynamic work counter of the density kernel
+    int32_t work_force;     // dynamic work counter of the force kernel
+    uint32_t err;           // error bits
+    int32_t err_index;      // first offending particle (best effort)
+    int32_t pad[23];
+};
+
+// Per-frame device pointers of one scene.
+struct Frame {
+    int n;
+    const float4 *pos_in, *vel_in, *ev_in;     // unsorted (previous order)
+    float4 *pos, *vel, *ev, *acc;              // sorted (current order)
+    uint32_t *key_in, *slot;                   // per source particle
+    unsigned long long *pairs;                 // (key << 32 | src), by cell
+    uint32_t *key;                             // sorted keys
+    int32_t *perm;                             // source of each sorted slot
+    int32_t *cell_count, *cell_start;
+    uint32_t *cell_xslab;
+    int32_t *occ_list, *big_list;
+    int4 *cell_val;                            // per occupied cell {req,sms,tra}
+    int4 *cell_prefix;                         // exclusive prefix of cell_val
+    gsph_block_task *tasks;
+    int32_t task_capacity;
+    int32_t *compact;
+    unsigned long long *scan_tiles;            // tile sums, cell scan
+    int4 *scan_tiles4;                         // tile sums, task scan
+    Counters *ctr;
+};
+
+// ---- launchers (grid.cu) ----
+void launch_hash_count(const Frame &f, const DevParams &P, cudaStream_t s);
+void launch_cell_scan(const Frame &f, const DevParams &P, cudaStream_t s);
+void launch_scatter_pairs(const Frame &f, cudaStream_t s);
+void launch_cell_sort(const Frame &f, int num_sms, cudaStream_t s);
+// ---- launchers (split.cu) ----
+void launch_split(const Frame &f, const DevParams &P, int max_occ,
+                  cudaStream_t s);
+// ---- launchers (physics.cu) ----
+void launch_density(const Frame &f, const DevParams &P, int num_sms,
+                    cudaStream_t s);
+void launch_force(const Frame &f, const DevParams &P, int num_sms,
+                  cudaStream_t s);
+void launch_integrate(const Frame &f, const DevParams &P, cudaStream_t s);
+void launch_reductions(const float4 *pos, const float4 *vel, int n,
+                       float mass, double *out8, cudaStream_t s);
+void launch_checksum(const float4 *pos, int n, double *out5, cudaStream_t s);
+
+// Host-side helpers (scene.cpp).
+DevParams make_dev_params(const gsph_params &p);
+void set_error(const char *fmt, ...);
+
+}  // namespace gsph
+
+#endif  // GSPH_INTERNAL_H_

@@ -1,0 +1,500 @@
+// physics.cu — density, force and integration (rows A10-A12), plus the FP64
+// state reductions.
+//
+// Reference behaviour (KemengHuang/Fast-General-GPU-SPH-framework):
+//   density    src/solver/density_kernels.cu:160-179 (TRA loop), 278-295
+//              (SMS batch), 297-565 (hybrid kernel; 1/rho -> position.w,
+//              pressure -> evaluated_velocity.w)
+//   force      src/solver/force_kernels.cu:378-435 (SMS batch), 525-561 (TRA
+//              loop), 725-1054 (hybrid kernel: spiky pressure, Mueller
+//              viscosity, colour-field surface tension -> acceleration)
+//   rows       src/solver/kernel_common.cuh:69-112 (TRA row range),
+//              614-674 (SMS row range from task micro bounds)
+//   integrate  src/solver/integration_kernels.cu:235-336 (knIntegrateVelocityE)
+//   checksum   src/simulation/sph_hybrid_system.cpp:43-62
+//
+// Design here: one persistent kernel per pass; each warp repeatedly takes a
+// work unit from a device counter — 32 TRA particles (one per lane) or one
+// 32-particle SMS task (candidates staged 32 at a time in shared memory and
+// broadcast to all lanes). The grid is sized from the SM count, so the launch
+// needs neither the host-side TRA/SMS counts nor a host synchronisation.
+// Neighbour rows merge the three x-adjacent cells of each (dy, dz) row into one
+// contiguous index range, pruned by micro-x slab as in the reference; the
+// interacting neighbours are visited in the same order (rows z-major, then
+// increasing sorted index), so sums match the reference's summation order.
+#include "gsph_internal.h"
+
+namespace gsph {
+
+namespace {
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
+constexpr float kFloatSmall = 1e-12f;   // core/cuda_math.cuh:14
+
+__device__ __forceinline__ float powf_7(float b) {
+    // kernel_common.cuh:51-55, six sequential multiplies
+    return b * b * b * b * b * b * b;
+}
+
+// Start of micro-x slab `lo` of cell c (0 = cell start).
+__device__ __forceinline__ int slab_begin(const Frame &f, int c, int s, int e,
+                                          int lo) {
+    if (lo == 0) return s;
+    const uint32_t xs = f.cell_xslab[c];
+    if (xs == kXslabUnknown) return s;
+    return s + min(int((xs >> (10 * (lo - 1))) & 1023u), e - s);
+}
+// End of micro-x slab `hi` of cell c (3 = cell end).
+__device__ __forceinline__ int slab_end(const Frame &f, int c, int s, int e,
+                                        int hi) {
+    if (hi == 3) return e;
+    const uint32_t xs = f.cell_xslab[c];
+    if (xs == kXslabUnknown) return e;
+    return s + min(int((xs >> (10 * hi)) & 1023u), e - s);
+}
+
+// Contiguous candidate range of one neighbour row: left cell from micro-x
+// `lo`, the middle cell, right cell up to micro-x `hi` (kernel_common.cuh:
+// 69-112 for TRA with lo = hi = own micro-x; 614-674 for SMS tasks).
+__device__ __forceinline__ void row_range(const Frame &f, const DevParams &P,
+                                          int m, int cx, int lo, int hi,
+                                          int &begin, int &end) {
+    const int sM = f.cell_start[m];
+    const int eM = f.cell_start[m + 1];
+    begin = sM;
+    end = eM;
+    if (cx > 0) begin = slab_begin(f, m - 1, f.cell_start[m - 1], sM, lo);
+    if (cx + 1 < P.gx) end = slab_end(f, m + 1, eM, f.cell_start[m + 2], hi);
+}
+
+struct MicroPos {
+    int cx, cy, cz, lmx;
+};
+
+__device__ __forceinline__ MicroPos micro_of(float4 p, const DevParams &P) {
+    // Same float arithmetic as the key (grid.cu); positions are inside the
+    // grid after the arrange stage has clamped/flagged them.
+    int mx = int(floorf(p.x * P.rat));
+    int my = int(floorf(p.y * P.rat));
+    int mz = int(floorf(p.z * P.rat));
+    mx = min(max(mx, 0), (P.gx << 2) - 1);
+    my = min(max(my, 0), (P.gy << 2) - 1);
+    mz = min(max(mz, 0), (P.gz << 2) - 1);
+    MicroPos r;
+    r.cx = mx >> 2;
+    r.cy = my >> 2;
+    r.cz = mz >> 2;
+    r.lmx = mx & 3;
+    return r;
+}
+
+__device__ __forceinline__ float density_pair(float4 self, float4 q, float h2) {
+    const float dx = self.x - q.x, dy = self.y - q.y, dz = self.z - q.z;
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    if (h2 < d2 || kFloatSmall > d2) return 0.f;
+    const float t = h2 - d2;
+    return t * t * t;
+}
+
+struct ForceAcc {
+    float px, py, pz;   // pressure sum
+    float vx, vy, vz;   // viscosity sum
+    float gx, gy, gz;   // colour gradient
+    float lap;          // colour laplacian
+};
+
+__device__ __forceinline__ void force_pair(const float4 &self,
+                                           const float4 &sev, const float4 &q,
+                                           const float4 &qev,
+                                           const DevParams &P, ForceAcc &a) {
+    const float rx = self.x - q.x, ry = self.y - q.y, rz = self.z - q.z;
+    const float d2 = rx * rx + ry * ry + rz * rz;
+    if (P.h2 < d2 || kFloatSmall > d2) return;
+    const float inv_d = rsqrtf(d2);
+    const float d = d2 * inv_d;
+    const float V = q.w;   // 1/rho_j
+    const float k = P.h - d;
+    const float wk = V * k;
+    const float pw = wk * (sev.w + qev.w) * k;
+    const float ps = pw * inv_d;
+    a.px -= rx * ps;
+    a.py -= ry * ps;
+    a.pz -= rz * ps;
+    a.vx += (qev.x - sev.x) * wk;
+    a.vy += (qev.y - sev.y) * wk;
+    a.vz += (qev.z - sev.z) * wk;
+    const float h2r2 = P.h2 - d2;
+    const float wh = V * h2r2;
+    const float gw = wh * h2r2;
+    a.gx += rx * gw;
+    a.gy += ry * gw;
+    a.gz += rz * gw;
+    a.lap += wh * (d2 - 0.75f * h2r2);
+}
+
+__device__ __forceinline__ void write_density(const Frame &f, const DevParams &P,
+                                              int self, float sum, bool sms) {
+    float rho = sum * P.density_scale + P.self_density;
+    // The SMS path of the reference guards rho < 1e-12 before the reciprocal
+    // (density_kernels.cu:540-541); the TRA path does not (:353-355).
+    const float stored = (sms && rho < kFloatSmall) ? P.rest_density : rho;
+    f.pos[self].w = __fdividef(1.0f, stored);
+    f.ev[self].w = (powf_7(rho * P.inv_rest_density) - 1) * P.gas_constant;
+}
+
+__device__ __forceinline__ void write_force(const Frame &f, const DevParams &P,
+                                            int self, float inv_rho,
+                                            const ForceAcc &a, bool sms) {
+    float tx = a.px * P.half_spiky + a.vx * P.visco_coef;
+    float ty = a.py * P.half_spiky + a.vy * P.visco_coef;
+    float tz = a.pz * P.half_spiky + a.vz * P.visco_coef;
+    const float gx = a.gx * P.grad_color_scale;
+    const float gy = a.gy * P.grad_color_scale;
+    const float gz = a.gz * P.grad_color_scale;
+    float lap = a.lap * P.lplc_color_scale;
+    lap *= inv_rho;
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    const float n2 = gx * gx + gy * gy + gz * gz;
+    if (sms) {
+        // force_kernels.cu:1030-1043
+        const float inv_n = rsqrtf(n2);
+        const float nrm = n2 * inv_n;
+        if (nrm > P.surface_normal) {
+            const float s = P.surface_coe * lap * inv_n;
+            sx = gx * s;
+            sy = gy * s;
+            sz = gz * s;
+        }
+    } else {
+        // force_kernels.cu:796-805
+        const float nrm = sqrtf(n2);
+        if (nrm > P.surface_normal) {
+            sx = gx * P.surface_coe * lap / nrm;
+            sy = gy * P.surface_coe * lap / nrm;
+            sz = gz * P.surface_coe * lap / nrm;
+        }
+    }
+    tx *= P.mass;
+    ty *= P.mass;
+    tz *= P.mass;
+    f.acc[self] = make_float4(tx + sx, ty + sy, tz + sz, 0.f);
+}
+
+constexpr int kWarpsPerBlock = 8;
+
+// ---------------------------------------------------------------- density --
+__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+k_density(Frame f, DevParams P) {
+    __shared__ float4 stage[kWarpsPerBlock][32];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int middle = f.ctr->middle;
+    const int task_count = f.ctr->task_count;
+    const int tra_units = (middle + 31) >> 5;
+    const int total = tra_units + task_count;
+    for (;;) {
+        int u = 0;
+        if (lane == 0) u = atomicAdd(&f.ctr->work_density, 1);
+        u = __shfl_sync(kFull, u, 0);
+        if (u >= total) break;
+        if (u < tra_units) {
+            // TRA: one particle per lane (density_kernels.cu:318-366).
+            const int idx = (u << 5) + lane;
+            if (idx >= middle) continue;
+            const int self = f.compact[idx];
+            const float4 p = f.pos[self];
+            const MicroPos mp = micro_of(p, P);
+            float sum = 0.f;
+            for (int r = 0; r < 9; ++r) {
+                const int ny = mp.cy + (r % 3) - 1;
+                const int nz = mp.cz + (r / 3) - 1;
+                if (ny < 0 || ny >= P.gy || nz < 0 || nz >= P.gz) continue;
+                const int m = mp.cx + P.gx * (ny + P.gy * nz);
+                int begin, end;
+                row_range(f, P, m, mp.cx, mp.lmx, mp.lmx, begin, end);
+                for (int j = begin; j < end; ++j)
+                    sum += density_pair(p, f.pos[j], P.h2);
+            }
+            write_density(f, P, self, sum, false);
+        } else {
+            // SMS: one 32-particle task per warp (density_kernels.cu:368-565).
+            const gsph_block_task task = f.tasks[u - tra_units];
+            const int cb = task.cell_begin;
+            const int cend = cb + task.cell_particle_count;
+            const int self = cb + task.p_offset + lane;
+            const bool active = self < cend;
+            if (cb + int(task.p_offset) >= cend) continue;   // warp-uniform
+            const float4 p = f.pos[active ? self : cend - 1];
+            const int cx = task.cell_pos[0], cy = task.cell_pos[1],
+                      cz = task.cell_pos[2];
+            float sum = 0.f;
+            for (int r = 0; r < 9; ++r) {
+                const int ny = cy + (r % 3) - 1;
+                const int nz = cz + (r / 3) - 1;
+                if (ny < 0 || ny >= P.gy || nz < 0 || nz >= P.gz) continue;
+                const int m = cx + P.gx * (ny + P.gy * nz);
+                int begin, end;
+                row_range(f, P, m, cx, task.xxi, task.xxx, begin, end);
+                for (int base = begin; base < end; base += 32) {
+                    const int cnt = min(32, end - base);
+                    if (lane < cnt) stage[warp][lane] = f.pos[base + lane];
+                    __syncwarp();
+                    for (int k = 0; k < cnt; ++k)
+                        sum += density_pair(p, stage[warp][k], P.h2);
+                    __syncwarp();
+                }
+            }
+            if (active) write_density(f, P, self, sum, true);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ force --
+__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+k_force(Frame f, DevParams P) {
+    __shared__ float4 stage_p[kWarpsPerBlock][32];
+    __shared__ float4 stage_v[kWarpsPerBlock][32];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int middle = f.ctr->middle;
+    const int task_count = f.ctr->task_count;
+    const int tra_units = (middle + 31) >> 5;
+    const int total = tra_units + task_count;
+    for (;;) {
+        int u = 0;
+        if (lane == 0) u = atomicAdd(&f.ctr->work_force, 1);
+        u = __shfl_sync(kFull, u, 0);
+        if (u >= total) break;
+        ForceAcc a = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (u < tra_units) {
+            const int idx = (u << 5) + lane;
+            if (idx >= middle) continue;
+            const int self = f.compact[idx];
+            const float4 p = f.pos[self];
+            const float4 pev = f.ev[self];
+            const MicroPos mp = micro_of(p, P);
+            for (int r = 0; r < 9; ++r) {
+                const int ny = mp.cy + (r % 3) - 1;
+                const int nz = mp.cz + (r / 3) - 1;
+                if (ny < 0 || ny >= P.gy || nz < 0 || nz >= P.gz) continue;
+                const int m = mp.cx + P.gx * (ny + P.gy * nz);
+                int begin, end;
+                row_range(f, P, m, mp.cx, mp.lmx, mp.lmx, begin, end);
+                for (int j = begin; j < end; ++j) {
+                    const float4 q = f.pos[j];
+                    const float rx = p.x - q.x, ry = p.y - q.y, rz = p.z - q.z;
+                    const float d2 = rx * rx + ry * ry + rz * rz;
+                    if (P.h2 < d2 || kFloatSmall > d2) continue;
+                    force_pair(p, pev, q, f.ev[j], P, a);
+                }
+            }
+            write_force(f, P, self, p.w, a, false);
+        } else {
+            const gsph_block_task task = f.tasks[u - tra_units];
+            const int cb = task.cell_begin;
+            const int cend = cb + task.cell_particle_count;
+            const int self = cb + task.p_offset + lane;
+            const bool active = self < cend;
+            if (cb + int(task.p_offset) >= cend) continue;
+            const int safe = active ? self : cend - 1;
+            const float4 p = f.pos[safe];
+            const float4 pev = f.ev[safe];
+            const int cx = task.cell_pos[0], cy = task.cell_pos[1],
+                      cz = task.cell_pos[2];
+            for (int r = 0; r < 9; ++r) {
+                const int ny = cy + (r % 3) - 1;
+                const int nz = cz + (r / 3) - 1;
+                if (ny < 0 || ny >= P.gy || nz < 0 || nz >= P.gz) continue;
+                const int m = cx + P.gx * (ny + P.gy * nz);
+                int begin, end;
+                row_range(f, P, m, cx, task.xxi, task.xxx, begin, end);
+                for (int base = begin; base < end; base += 32) {
+                    const int cnt = min(32, end - base);
+                    if (lane < cnt) {
+                        stage_p[warp][lane] = f.pos[base + lane];
+                        stage_v[warp][lane] = f.ev[base + lane];
+                    }
+                    __syncwarp();
+                    for (int k = 0; k < cnt; ++k)
+                        force_pair(p, pev, stage_p[warp][k], stage_v[warp][k], P, a);
+                    __syncwarp();
+                }
+            }
+            if (active) write_force(f, P, self, p.w, a, true);
+        }
+    }
+}
+
+// -------------------------------------------------------------- integrate --
+// knIntegrateVelocityE (integration_kernels.cu:235-336), same operation order.
+__global__ void __launch_bounds__(256)
+k_integrate(Frame f, DevParams P) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= f.n) return;
+    const float4 tp = f.pos[i];
+    const float4 ev = f.ev[i];
+    const float4 v4 = f.vel[i];
+    const float4 a4 = f.acc[i];
+    float vx = v4.x, vy = v4.y, vz = v4.z;
+    float ax = a4.x, ay = a4.y, az = a4.z;
+    const float alpha = 20000000.f;
+    const float beta = 200000.f;
+    const float kernel = P.wall_kernel;
+    float diff;
+    diff = kernel - (tp.y - P.bmin_y);
+    if (diff > 0.0f) ay += alpha * diff - beta * vy;
+    diff = kernel - (P.bmax_y - tp.y);
+    if (diff > 0.0f) ay -= alpha * diff + beta * vy;
+    diff = kernel - (tp.x - P.bmin_x);
+    if (diff > 0.0f) ax += alpha * diff - beta * vx;
+    diff = kernel - (P.bmax_x - tp.x);
+    if (diff > 0.0f) ax -= alpha * diff + beta * vx;
+    diff = kernel - (tp.z - P.bmin_z);
+    if (diff > 0.0f) az += alpha * diff - beta * vz;
+    diff = kernel - (P.bmax_z - tp.z);
+    if (diff > 0.0f) az -= alpha * diff + beta * vz;
+    const float acc_limit = 3000000.f;
+    const float vel_limit = 36.f;
+    ax = ax * tp.w + P.gx_acc;
+    ay = ay * tp.w + P.gy_acc;
+    az = az * tp.w + P.gz_acc;
+    float speed = ax * ax + ay * ay + az * az;
+    if (speed > acc_limit) {
+        const float s = sqrtf(acc_limit / speed);
+        ax *= s;
+        ay *= s;
+        az *= s;
+    }
+    vx += ax * P.time_step;
+    vy += ay * P.time_step;
+    vz += az * P.time_step;
+    speed = vx * vx + vy * vy + vz * vz;
+    if (speed > vel_limit) {
+        const float s = sqrtf(vel_limit / speed);
+        vx *= s;
+        vy *= s;
+        vz *= s;
+    }
+    float px = tp.x + vx * P.time_step;
+    float py = tp.y + vy * P.time_step;
+    float pz = tp.z + vz * P.time_step;
+    if (px >= P.bmax_x) { vx *= P.wall_damping; px = P.bmax_x - kernel; }
+    if (px <= P.bmin_x) { vx *= P.wall_damping; px = P.bmin_x + kernel; }
+    if (py >= P.bmax_y) { vy *= P.wall_damping; py = P.bmax_y - kernel; }
+    if (py <= P.bmin_y) { vy *= P.wall_damping; py = P.bmin_y + kernel; }
+    if (pz >= P.bmax_z) { vz *= P.wall_damping; pz = P.bmax_z - kernel; }
+    if (pz <= P.bmin_z) { vz *= P.wall_damping; pz = P.bmin_z + kernel; }
+    f.pos[i] = make_float4(px, py, pz, tp.w);
+    f.vel[i] = make_float4(vx, vy, vz, 0.f);
+    f.ev[i] = make_float4((vx + ev.x) * 0.5f, (vy + ev.y) * 0.5f,
+                          (ev.z + vz) * 0.5f, ev.w);
+}
+
+// ------------------------------------------------------- FP64 reductions --
+// Deterministic two-level tree: fixed per-block partials, then one block.
+constexpr int kRedThreads = 256;
+constexpr int kRedBlocks = 512;
+
+template <int K>
+__device__ __forceinline__ void block_sum(double (&v)[K], double *out) {
+    __shared__ double sh[K][kRedThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double x = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(kFull, x, o);
+        if (lane == 0) sh[k][warp] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+        double t = 0.0;
+        for (int w = 0; w < kRedThreads / 32; ++w) t += sh[threadIdx.x][w];
+        out[threadIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(kRedThreads)
+k_checksum_partial(const float4 *__restrict__ pos, int n,
+                   double *__restrict__ part) {
+    double v[5] = {0, 0, 0, 0, 0};
+    for (int i = blockIdx.x * kRedThreads + threadIdx.x; i < n;
+         i += gridDim.x * kRedThreads) {
+        const float4 p = pos[i];
+        v[0] += p.x;
+        v[1] += p.y;
+        v[2] += p.z;
+        v[3] += p.w;
+        v[4] += double((unsigned(i) & 1023u) + 1u) *
+                (double(p.x) + 3.0 * double(p.y) + 7.0 * double(p.z));
+    }
+    block_sum<5>(v, part + 5 * blockIdx.x);
+}
+
+__global__ void __launch_bounds__(kRedThreads)
+k_reduce_partial(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+                 int n, double mass, double *__restrict__ part) {
+    double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int i = blockIdx.x * kRedThreads + threadIdx.x; i < n;
+         i += gridDim.x * kRedThreads) {
+        const float4 p = pos[i];
+        const float4 u = vel[i];
+        v[0] += mass;
+        v[1] += mass * u.x;
+        v[2] += mass * u.y;
+        v[3] += mass * u.z;
+        v[4] += 0.5 * mass * (double(u.x) * u.x + double(u.y) * u.y +
+                              double(u.z) * u.z);
+        v[5] += p.x;
+        v[6] += p.y;
+        v[7] += p.z;
+    }
+    block_sum<8>(v, part + 8 * blockIdx.x);
+}
+
+template <int K>
+__global__ void __launch_bounds__(kRedThreads)
+k_final_sum(const double *__restrict__ part, int nparts, double *__restrict__ out) {
+    double v[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = 0.0;
+    for (int b = threadIdx.x; b < nparts; b += kRedThreads)
+#pragma unroll
+        for (int k = 0; k < K; ++k) v[k] += part[K * b + k];
+    block_sum<K>(v, out);
+}
+
+}  // namespace
+
+void launch_density(const Frame &f, const DevParams &P, int num_sms,
+                    cudaStream_t s) {
+    if (f.n <= 0) return;
+    k_density<<<num_sms * 8, kWarpsPerBlock * 32, 0, s>>>(f, P);
+}
+
+void launch_force(const Frame &f, const DevParams &P, int num_sms,
+                  cudaStream_t s) {
+    if (f.n <= 0) return;
+    k_force<<<num_sms * 8, kWarpsPerBlock * 32, 0, s>>>(f, P);
+}
+
+void launch_integrate(const Frame &f, const DevParams &P, cudaStream_t s) {
+    if (f.n <= 0) return;
+    k_integrate<<<(f.n + 255) / 256, 256, 0, s>>>(f, P);
+}
+
+// out5 must hold 5 + 5*kRedBlocks doubles (partials follow the result).
+void launch_checksum(const float4 *pos, int n, double *out5, cudaStream_t s) {
+    k_checksum_partial<<<kRedBlocks, kRedThreads, 0, s>>>(pos, n, out5 + 8);
+    k_final_sum<5><<<1, kRedThreads, 0, s>>>(out5 + 8, kRedBlocks, out5);
+}
+
+// out8 must hold 8 + 8*kRedBlocks doubles.
+void launch_reductions(const float4 *pos, const float4 *vel, int n, float mass,
+                       double *out8, cudaStream_t s) {
+    k_reduce_partial<<<kRedBlocks, kRedThreads, 0, s>>>(pos, vel, n, mass,
+                                                        out8 + 8);
+    k_final_sum<8><<<1, kRedThreads, 0, s>>>(out8 + 8, kRedBlocks, out8);
+}
+
+}  // namespace gsph

@@ -1,0 +1,951 @@
+// system.cu — the scene runtime behind the C ABI: device buffers, the frame
+// (tick) pipeline, CUDA-graph capture, timing, checksums and copy-out.
+//
+// Reference counterparts (KemengHuang/Fast-General-GPU-SPH-framework):
+//   HybridSystem ctor / initializeScene  src/simulation/sph_hybrid_system.cpp:209-240, 432-473
+//   HybridSystem::tick                   src/simulation/sph_hybrid_system.cpp:253-339
+//   HybridSystem::runBenchmark           src/simulation/sph_hybrid_system.cpp:341-430
+//   Arrangement ctor (buffers)           src/grid/sph_arrangement.cu:607-673
+//   Arrangement::arrangeHybridFrame      src/grid/sph_arrangement.cu:1493-1506
+//   getSmsTaskPairStats                  src/grid/sph_arrangement.cu:1595-1636
+//   knInit (zero ev, acc)                src/solver/integration_kernels.cu:6-17
+//
+// Unlike the reference, a frame needs no host synchronisation (the TRA/SMS
+// counts stay on the device), so whole frames can be captured as CUDA graphs.
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "gsph_internal.h"
+
+namespace gsph {
+
+namespace {
+
+#define GSPH_CUDA(call)                                                         \
+    do {                                                                        \
+        cudaError_t e_ = (call);                                                \
+        if (e_ != cudaSuccess) {                                                \
+            set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_),  \
+                      __FILE__, __LINE__);                                      \
+            return GSPH_ERR_CUDA;                                               \
+        }                                                                       \
+    } while (0)
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+int device_sm_count(int device) {
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device) !=
+            cudaSuccess ||
+        v <= 0)
+        v = 1;
+    return v;
+}
+
+}  // namespace
+
+struct System {
+    gsph_params params{};
+    DevParams dp{};
+    int device = 0;
+    int num_sms = 1;
+    int n = 0;
+    int numc = 0;
+    int max_occ = 0;
+    int task_capacity = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<void *> allocs;
+    size_t device_bytes = 0;
+
+    float4 *pos[2] = {nullptr, nullptr};
+    float4 *vel[2] = {nullptr, nullptr};
+    float4 *ev[2] = {nullptr, nullptr};
+    float4 *acc = nullptr;
+    int cur = 0;   // buffer index that holds the current (sorted) state
+    Frame fr{};    // pointers shared by both parities
+    double *red = nullptr;   // reductions workspace
+    bool arranged = false;   // sorted state + split valid
+    uint64_t frames = 0;
+
+    bool graph_mode = false;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::vector<cudaEvent_t>> ev_pending;   // 5 events per frame
+
+    ~System() { release(); }
+
+    void release() {
+        if (device >= 0) cudaSetDevice(device);
+        for (auto &g : graph)
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
+        for (auto &v : ev_pending)
+            for (auto e : v) cudaEventDestroy(e);
+        ev_pending.clear();
+        for (auto e : ev_pool) cudaEventDestroy(e);
+        ev_pool.clear();
+        for (void *p : allocs) cudaFree(p);
+        allocs.clear();
+        if (stream) {
+            cudaStreamDestroy(stream);
+            stream = nullptr;
+        }
+    }
+
+    gsph_status alloc(void **p, size_t bytes) {
+        bytes = std::max<size_t>(align_up(bytes, 256), 256);
+        cudaError_t e = cudaMalloc(p, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            set_error("cudaMalloc of %zu bytes failed: %s", bytes,
+                      cudaGetErrorString(e));
+            return e == cudaErrorMemoryAllocation ? GSPH_ERR_OUT_OF_MEMORY
+                                                  : GSPH_ERR_CUDA;
+        }
+        allocs.push_back(*p);
+        device_bytes += bytes;
+        return GSPH_OK;
+    }
+
+    template <typename T>
+    gsph_status alloc_n(T **p, size_t count) {
+        return alloc(reinterpret_cast<void **>(p), count * sizeof(T));
+    }
+
+    gsph_status init(const gsph_params &p, const float *pos4, const float *vel4,
+                     int count, int dev) {
+        params = p;
+        dp = make_dev_params(p);
+        device = dev;
+        n = count;
+        numc = dp.numc;
+        GSPH_CUDA(cudaSetDevice(device));
+        num_sms = device_sm_count(device);
+        GSPH_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        max_occ = std::max(1, std::min(numc, n));
+        task_capacity = (n + kSmsTaskParticles - 1) / kSmsTaskParticles +
+                        max_occ + 2;
+        const size_t N = size_t(std::max(n, 1));
+        gsph_status st;
+        for (int b = 0; b < 2; ++b) {
+            if ((st = alloc_n(&pos[b], N)) || (st = alloc_n(&vel[b], N)) ||
+                (st = alloc_n(&ev[b], N)))
+                return st;
+        }
+        if ((st = alloc_n(&acc, N)) || (st = alloc_n(&fr.key_in, N)) ||
+            (st = alloc_n(&fr.slot, N)) || (st = alloc_n(&fr.pairs, N)) ||
+            (st = alloc_n(&fr.key, N)) || (st = alloc_n(&fr.perm, N)) ||
+            (st = alloc_n(&fr.cell_count, size_t(numc))) ||
+            (st = alloc_n(&fr.cell_start, size_t(numc) + 1)) ||
+            (st = alloc_n(&fr.cell_xslab, size_t(numc))) ||
+            (st = alloc_n(&fr.occ_list, size_t(max_occ))) ||
+            (st = alloc_n(&fr.big_list, size_t(max_occ))) ||
+            (st = alloc_n(&fr.cell_val, size_t(max_occ))) ||
+            (st = alloc_n(&fr.cell_prefix, size_t(max_occ))) ||
+            (st = alloc_n(&fr.tasks, size_t(task_capacity))) ||
+            (st = alloc_n(&fr.compact, N)) ||
+            (st = alloc_n(&fr.scan_tiles,
+                          size_t((numc + kScanTile - 1) / kScanTile))) ||
+            (st = alloc_n(&fr.scan_tiles4,
+                          size_t((max_occ + kScanTile - 1) / kScanTile))) ||
+            (st = alloc_n(&fr.ctr, 1)) ||
+            (st = alloc_n(&red, size_t(8 + 8 * 512))))
+            return st;
+        fr.n = n;
+        fr.acc = acc;
+        fr.task_capacity = task_capacity;
+        GSPH_CUDA(cudaMemsetAsync(fr.cell_count, 0, sizeof(int32_t) * numc, stream));
+        GSPH_CUDA(cudaMemsetAsync(fr.cell_xslab, 0xFF, sizeof(uint32_t) * numc, stream));
+        GSPH_CUDA(cudaMemsetAsync(fr.ctr, 0, sizeof(Counters), stream));
+        GSPH_CUDA(cudaMemsetAsync(fr.tasks, 0, sizeof(gsph_block_task) * task_capacity, stream));
+        for (int b = 0; b < 2; ++b) {
+            GSPH_CUDA(cudaMemsetAsync(pos[b], 0, sizeof(float4) * N, stream));
+            GSPH_CUDA(cudaMemsetAsync(vel[b], 0, sizeof(float4) * N, stream));
+            GSPH_CUDA(cudaMemsetAsync(ev[b], 0, sizeof(float4) * N, stream));
+        }
+        GSPH_CUDA(cudaMemsetAsync(acc, 0, sizeof(float4) * N, stream));
+        if (n > 0) {
+            GSPH_CUDA(cudaMemcpyAsync(pos[0], pos4, sizeof(float4) * n,
+                                      cudaMemcpyHostToDevice, stream));
+            if (vel4)
+                GSPH_CUDA(cudaMemcpyAsync(vel[0], vel4, sizeof(float4) * n,
+                                          cudaMemcpyHostToDevice, stream));
+        }
+        cur = 0;
+        GSPH_CUDA(cudaStreamSynchronize(stream));
+        return GSPH_OK;
+    }
+
+    // Frame descriptor of the arrange stage reading buffer `in`.
+    Frame frame_arrange(int in) const {
+        Frame f = fr;
+        f.pos_in = pos[in];
+        f.vel_in = vel[in];
+        f.ev_in = ev[in];
+        f.pos = pos[1 - in];
+        f.vel = vel[1 - in];
+        f.ev = ev[1 - in];
+        return f;
+    }
+    // Frame descriptor of the physics stages on buffer `b`.
+    Frame frame_physics(int b) const {
+        Frame f = fr;
+        f.pos_in = pos[b];
+        f.vel_in = vel[b];
+        f.ev_in = ev[b];
+        f.pos = pos[b];
+        f.vel = vel[b];
+        f.ev = ev[b];
+        return f;
+    }
+
+    void enqueue_arrange(int in) {
+        const Frame f = frame_arrange(in);
+        launch_hash_count(f, dp, stream);
+        launch_cell_scan(f, dp, stream);
+        launch_scatter_pairs(f, stream);
+        launch_cell_sort(f, num_sms, stream);
+        launch_split(f, dp, max_occ, stream);
+    }
+    void enqueue_density(int b) { launch_density(frame_physics(b), dp, num_sms, stream); }
+    void enqueue_force(int b) { launch_force(frame_physics(b), dp, num_sms, stream); }
+    void enqueue_advance(int b) { launch_integrate(frame_physics(b), dp, stream); }
+
+    gsph_status check_launch() {
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            set_error("kernel launch failed: %s", cudaGetErrorString(e));
+            return GSPH_ERR_CUDA;
+        }
+        return GSPH_OK;
+    }
+
+    cudaEvent_t take_event() {
+        if (!ev_pool.empty()) {
+            cudaEvent_t e = ev_pool.back();
+            ev_pool.pop_back();
+            return e;
+        }
+        cudaEvent_t e = nullptr;
+        cudaEventCreate(&e);
+        return e;
+    }
+
+    gsph_status build_graph(int parity) {
+        cudaGraph_t g = nullptr;
+        GSPH_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_arrange(parity);
+        enqueue_density(1 - parity);
+        enqueue_force(1 - parity);
+        enqueue_advance(1 - parity);
+        cudaError_t e = cudaStreamEndCapture(stream, &g);
+        if (e != cudaSuccess) {
+            set_error("graph capture failed: %s", cudaGetErrorString(e));
+            if (g) cudaGraphDestroy(g);
+            return GSPH_ERR_CUDA;
+        }
+        e = cudaGraphInstantiate(&graph[parity], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            set_error("graph instantiate failed: %s", cudaGetErrorString(e));
+            graph[parity] = nullptr;
+            return GSPH_ERR_CUDA;
+        }
+        return GSPH_OK;
+    }
+
+    gsph_status tick() {
+        const int in = cur, out = 1 - cur;
+        if (graph_mode && !timing) {
+            if (!graph[in]) {
+                gsph_status st = build_graph(in);
+                if (st) return st;
+            }
+            GSPH_CUDA(cudaGraphLaunch(graph[in], stream));
+        } else {
+            std::vector<cudaEvent_t> evs;
+            if (timing) {
+                for (int k = 0; k < 5; ++k) evs.push_back(take_event());
+                cudaEventRecord(evs[0], stream);
+            }
+            enqueue_arrange(in);
+            if (timing) cudaEventRecord(evs[1], stream);
+            enqueue_density(out);
+            if (timing) cudaEventRecord(evs[2], stream);
+            enqueue_force(out);
+            if (timing) cudaEventRecord(evs[3], stream);
+            enqueue_advance(out);
+            if (timing) {
+                cudaEventRecord(evs[4], stream);
+                ev_pending.push_back(std::move(evs));
+            }
+            gsph_status st = check_launch();
+            if (st) return st;
+        }
+        cur = out;
+        arranged = true;
+        ++frames;
+        return GSPH_OK;
+    }
+
+    gsph_status read_counters(Counters &c) {
+        GSPH_CUDA(cudaMemcpyAsync(&c, fr.ctr, sizeof(Counters),
+                                  cudaMemcpyDeviceToHost, stream));
+        GSPH_CUDA(cudaStreamSynchronize(stream));
+        return GSPH_OK;
+    }
+
+    gsph_status sync_and_check() {
+        GSPH_CUDA(cudaStreamSynchronize(stream));
+        Counters c;
+        gsph_status st = read_counters(c);
+        if (st) return st;
+        if (c.err & kErrOutOfDomain) {
+            set_error("a particle left the simulation grid (first index %d); it "
+                      "was clamped into the boundary cell",
+                      c.err_index);
+            clear_err();
+            return GSPH_ERR_DOMAIN;
+        }
+        if (c.err & kErrTaskCapacity) {
+            set_error("SMS task buffer overflow");
+            clear_err();
+            return GSPH_ERR_CAPACITY;
+        }
+        return GSPH_OK;
+    }
+
+    void clear_err() {
+        uint32_t z[2] = {0, 0};
+        cudaMemcpyAsync(&fr.ctr->err, z, sizeof(z), cudaMemcpyHostToDevice, stream);
+        cudaStreamSynchronize(stream);
+    }
+
+    gsph_status stage_times(float out[4]) {
+        GSPH_CUDA(cudaStreamSynchronize(stream));
+        double acc4[4] = {0, 0, 0, 0};
+        const size_t nf = ev_pending.size();
+        for (auto &evs : ev_pending) {
+            for (int k = 0; k < 4; ++k) {
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, evs[k], evs[k + 1]);
+                acc4[k] += ms;
+            }
+            for (auto e : evs) ev_pool.push_back(e);
+        }
+        ev_pending.clear();
+        for (int k = 0; k < 4; ++k) out[k] = nf ? float(acc4[k] / nf) : 0.f;
+        return GSPH_OK;
+    }
+};
+
+}  // namespace gsph
+
+using namespace gsph;
+
+struct gsph_system {
+    System sys;
+};
+
+namespace {
+
+gsph_status check_handle(gsph_handle h) {
+    if (!h) {
+        set_error("null gsph handle");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    cudaError_t e = cudaSetDevice(h->sys.device);
+    if (e != cudaSuccess) {
+        set_error("cudaSetDevice(%d) failed: %s", h->sys.device,
+                  cudaGetErrorString(e));
+        return GSPH_ERR_CUDA;
+    }
+    return GSPH_OK;
+}
+
+size_t field_bytes(const System &s, gsph_field f, gsph_status &st) {
+    st = GSPH_OK;
+    const size_t N = size_t(s.n);
+    switch (f) {
+        case GSPH_FIELD_POSITION:
+        case GSPH_FIELD_VELOCITY:
+        case GSPH_FIELD_EVAL_VELOCITY:
+        case GSPH_FIELD_ACCELERATION: return N * sizeof(float4);
+        case GSPH_FIELD_KEY:
+        case GSPH_FIELD_PERMUTATION:
+        case GSPH_FIELD_COMPACT_INDEX: return N * 4;
+        case GSPH_FIELD_CELL_START: return (size_t(s.numc) + 1) * 4;
+        case GSPH_FIELD_CELL_COUNT:
+        case GSPH_FIELD_BLOCK_REQ: return size_t(s.numc) * 4;
+        case GSPH_FIELD_MICRO_START: return (size_t(s.numc) * 64 + 1) * 4;
+        case GSPH_FIELD_SPLIT: return 8;
+        case GSPH_FIELD_TASKS: return 0;   // variable, checked separately
+    }
+    st = GSPH_ERR_INVALID_ARG;
+    set_error("unknown field %d", int(f));
+    return 0;
+}
+
+float4 *state_ptr(System &s, gsph_field f) {
+    switch (f) {
+        case GSPH_FIELD_POSITION: return s.pos[s.cur];
+        case GSPH_FIELD_VELOCITY: return s.vel[s.cur];
+        case GSPH_FIELD_EVAL_VELOCITY: return s.ev[s.cur];
+        case GSPH_FIELD_ACCELERATION: return s.acc;
+        default: return nullptr;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+gsph_status gsph_create(const gsph_params *p, const float *pos4,
+                        const float *vel4, uint32_t n, int device,
+                        gsph_handle *out) {
+    if (!p || !out || (n > 0 && !pos4)) {
+        set_error("gsph_create: null argument");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    if (n > 0x7FFFFFFFu) {
+        set_error("gsph_create: %u particles exceed 2^31-1", n);
+        return GSPH_ERR_CAPACITY;
+    }
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        set_error("There is no CUDA device (%s).",
+                  e == cudaSuccess ? "count 0" : cudaGetErrorString(e));
+        return GSPH_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= count) {
+        set_error("device %d out of range [0, %d)", device, count);
+        return GSPH_ERR_INVALID_ARG;
+    }
+    const int numc = p->grid_size[0] * p->grid_size[1] * p->grid_size[2];
+    if (numc <= 0 || p->grid_size[0] <= 0 || p->grid_size[1] <= 0 ||
+        p->grid_size[2] <= 0) {
+        set_error("gsph_create: empty grid");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    gsph_system *h = new (std::nothrow) gsph_system();
+    if (!h) {
+        set_error("gsph_create: host allocation failed");
+        return GSPH_ERR_OUT_OF_MEMORY;
+    }
+    gsph_status st = h->sys.init(*p, pos4, vel4, int(n), device);
+    if (st) {
+        delete h;
+        return st;
+    }
+    *out = h;
+    return GSPH_OK;
+}
+
+gsph_status gsph_create_from_json(const char *scene_path, int device,
+                                  gsph_handle *out) {
+    if (!scene_path || !out) {
+        set_error("gsph_create_from_json: null argument");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    gsph_scene sc;
+    gsph_status st = gsph_scene_load_json(scene_path, &sc);
+    if (st) return st;
+    gsph_params p;
+    if ((st = gsph_params_init(&sc, &p))) return st;
+    uint32_t n = 0;
+    if ((st = gsph_lattice_count(&sc, &p, &n))) return st;
+    std::vector<float> pos(size_t(n) * 4 + 4);
+    if ((st = gsph_lattice_fill(&sc, &p, pos.data(), n, &n))) return st;
+    return gsph_create(&p, pos.data(), nullptr, n, device, out);
+}
+
+gsph_status gsph_destroy(gsph_handle h) {
+    if (!h) return GSPH_OK;
+    delete h;
+    return GSPH_OK;
+}
+
+gsph_status gsph_step(gsph_handle h, int n_steps) {
+    gsph_status st = check_handle(h);
+    if (st) return st;
+    if (n_steps < 0) {
+        set_error("gsph_step: negative step count");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    for (int i = 0; i < n_steps; ++i)
+        if ((st = h->sys.tick())) return st;
+    return GSPH_OK;
+}
+
+gsph_status gsph_arrange(gsph_handle h) {
+    gsph_status st = check_handle(h);
+    if (st) return st;
+    System &s = h->sys;
+    s.enqueue_arrange(s.cur);
+    if ((st = s.check_launch())) return st;
+    s.cur = 1 - s.cur;
+    s.arranged = true;
+    return GSPH_OK;
+}
+
+static gsph_status need_arranged(System &s) {
+    if (!s.arranged) {
+        set_error("the grid has not been arranged yet (call gsph_arrange)");
+        return GSPH_ERR_STATE;
+    }
+    return GSPH_OK;
+}
+
+gsph_status gsph_density(gsph_handle h) {
+    gsph_status st = check_handle(h);
+    if (st || (st = need_arranged(h->sys))) return st;
+    h->sys.enqueue_density(h->sys.cur);
+    return h->sys.check_launch();
+}
+
+gsph_status gsph_force(gsph_handle h) {
+    gsph_status st = check_handle(h);
+    if (st || (st = need_arranged(h->sys))) return st;
+    h->sys.enqueue_force(h->sys.cur);
+    return h->sys.check_launch();
+}
+
+gsph_status gsph_advance(gsph_handle h) {
+    gsph_status st = check_handle(h);
+    if (st) return st;
+    h->sys.enqueue_advance(h->sys.cur);
+    return h->sys.check_launch();
+}
+
+gsph_status gsph_set_graph_mode(gsph_handle h, int enabled) {
+    gsph_status st = check_handle(h);
+    if (st) return st;
+    h->sys.graph_mode = enabled != 0;
+    return GSPH_OK;
+}
+
+gsph_status gsph_sync(gsph_handle h) {
+    gsph_status st = check_handle(h);
+    if (st) return st;
+    return h->sys.sync_and_check();
+}
+
+gsph_status gsph_stream(gsph_handle h, void **stream_out) {
+    if (!h || !stream_out) {
+        set_error("gsph_stream: null argument");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    *stream_out = static_cast<void *>(h->sys.stream);
+    return GSPH_OK;
+}
+
+gsph_status gsph_get_info(gsph_handle h, gsph_info *out) {
+    gsph_status st = check_handle(h);
+    if (st) return st;
+    if (!out) {
+        set_error("gsph_get_info: null output");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    System &s = h->sys;
+    Counters c;
+    if ((st = s.read_counters(c))) return st;
+    std::memset(out, 0, sizeof(*out));
+    out->n_particles = uint32_t(s.n);
+    out->n_cells = uint32_t(s.numc);
+    for (int a = 0; a < 3; ++a) out->grid_size[a] = s.params.grid_size[a];
+    out->tra_particles = s.arranged ? c.middle : s.n;
+    out->sms_tasks = s.arranged ? c.task_count : 0;
+    out->occupied_cells = c.num_occ;
+    out->big_cells = c.num_big;
+    out->frames = s.frames;
+    out->device_bytes = s.device_bytes;
+    return GSPH_OK;
+}
+
+gsph_status gsph_get_params(gsph_handle h, gsph_params *out) {
+    if (!h || !out) {
+        set_error("gsph_get_params: null argument");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    *out = h->sys.params;
+    return GSPH_OK;
+}
+
+gsph_status gsph_copy_out(gsph_handle h, gsph_field field, void *host_dst,
+                          size_t bytes) {
+    gsph_status st = check_handle(h);
+    if (st) return st;
+    if (!host_dst) {
+        set_error("gsph_copy_out: null destination");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    System &s = h->sys;
+    if ((st = s.sync_and_check()) && st != GSPH_ERR_DOMAIN) return st;
+    Counters c;
+    if ((st = s.read_counters(c))) return st;
+    const int T = s.arranged ? c.task_count : 0;
+    if (field == GSPH_FIELD_TASKS) {
+        const size_t need = size_t(T + (T & 1)) * sizeof(gsph_block_task);
+        if (bytes != need) {
+            set_error("gsph_copy_out(TASKS): %zu bytes given, %zu needed", bytes,
+                      need);
+            return GSPH_ERR_INVALID_ARG;
+        }
+        if (need)
+            GSPH_CUDA(cudaMemcpy(host_dst, s.fr.tasks, need, cudaMemcpyDeviceToHost));
+        return GSPH_OK;
+    }
+    const size_t need = field_bytes(s, field, st);
+    if (st) return st;
+    if (bytes != need) {
+        set_error("gsph_copy_out(%d): %zu bytes given, %zu needed", int(field),
+                  bytes, need);
+        return GSPH_ERR_INVALID_ARG;
+    }
+    const int numc = s.numc;
+    switch (field) {
+        case GSPH_FIELD_POSITION:
+        case GSPH_FIELD_VELOCITY:
+        case GSPH_FIELD_EVAL_VELOCITY:
+        case GSPH_FIELD_ACCELERATION:
+            if (need)
+                GSPH_CUDA(cudaMemcpy(host_dst, state_ptr(s, field), need,
+                                     cudaMemcpyDeviceToHost));
+            return GSPH_OK;
+        case GSPH_FIELD_KEY:
+            if (need) GSPH_CUDA(cudaMemcpy(host_dst, s.fr.key, need, cudaMemcpyDeviceToHost));
+            return GSPH_OK;
+        case GSPH_FIELD_PERMUTATION:
+            if (need) GSPH_CUDA(cudaMemcpy(host_dst, s.fr.perm, need, cudaMemcpyDeviceToHost));
+            return GSPH_OK;
+        case GSPH_FIELD_COMPACT_INDEX:
+            if (need) GSPH_CUDA(cudaMemcpy(host_dst, s.fr.compact, need, cudaMemcpyDeviceToHost));
+            return GSPH_OK;
+        case GSPH_FIELD_CELL_START:
+            GSPH_CUDA(cudaMemcpy(host_dst, s.fr.cell_start, need, cudaMemcpyDeviceToHost));
+            return GSPH_OK;
+        case GSPH_FIELD_CELL_COUNT: {
+            std::vector<int32_t> st1(size_t(numc) + 1);
+            GSPH_CUDA(cudaMemcpy(st1.data(), s.fr.cell_start, st1.size() * 4,
+                                 cudaMemcpyDeviceToHost));
+            int32_t *o = static_cast<int32_t *>(host_dst);
+            for (int i = 0; i < numc; ++i) o[i] = st1[i + 1] - st1[i];
+            return GSPH_OK;
+        }
+        case GSPH_FIELD_MICRO_START: {
+            // Dense micro offsets (the reference's d_cell_offset_M) rebuilt
+            // from the sorted keys: exclusive sum of the micro counts.
+            std::vector<uint32_t> keys(size_t(s.n));
+            if (s.n)
+                GSPH_CUDA(cudaMemcpy(keys.data(), s.fr.key, size_t(s.n) * 4,
+                                     cudaMemcpyDeviceToHost));
+            int32_t *o = static_cast<int32_t *>(host_dst);
+            const size_t m = size_t(numc) * 64;
+            std::memset(o, 0, (m + 1) * 4);
+            for (uint32_t k : keys)
+                if (k < m) ++o[k + 1];
+            for (size_t i = 1; i <= m; ++i) o[i] += o[i - 1];
+            return GSPH_OK;
+        }
+        case GSPH_FIELD_BLOCK_REQ: {
+            int32_t *o = static_cast<int32_t *>(host_dst);
+            std::memset(o, 0, size_t(numc) * 4);
+            if (!s.arranged || c.num_occ <= 0) return GSPH_OK;
+            std::vector<int32_t> occ(size_t(c.num_occ));
+            std::vector<int4> val(size_t(c.num_occ));
+            GSPH_CUDA(cudaMemcpy(occ.data(), s.fr.occ_list, occ.size() * 4,
+                                 cudaMemcpyDeviceToHost));
+            GSPH_CUDA(cudaMemcpy(val.data(), s.fr.cell_val, val.size() * sizeof(int4),
+                                 cudaMemcpyDeviceToHost));
+            for (size_t k = 0; k < occ.size(); ++k) o[occ[k]] = val[k].x;
+            return GSPH_OK;
+        }
+        case GSPH_FIELD_SPLIT: {
+            int32_t *o = static_cast<int32_t *>(host_dst);
+            o[0] = s.arranged ? c.middle : s.n;
+            o[1] = T;
+            return GSPH_OK;
+        }
+        default: break;
+    }
+    set_error("gsph_copy_out: unsupported field %d", int(field));
+    return GSPH_ERR_INVALID_ARG;
+}
+
+gsph_status gsph_copy_in(gsph_handle h, gsph_field field, const void *host_src,
+                         size_t bytes) {
+    gsph_status st = check_handle(h);
+    if (st) return st;
+    System &s = h->sys;
+    float4 *dst = state_ptr(s, field);
+    if (!dst || !host_src) {
+        set_error("gsph_copy_in: field %d is not writable or source is null",
+                  int(field));
+        return GSPH_ERR_INVALID_ARG;
+    }
+    if (bytes != size_t(s.n) * sizeof(float4)) {
+        set_error("gsph_copy_in: %zu bytes given, %zu needed", bytes,
+                  size_t(s.n) * sizeof(float4));
+        return GSPH_ERR_INVALID_ARG;
+    }
+    GSPH_CUDA(cudaStreamSynchronize(s.stream));
+    if (bytes) GSPH_CUDA(cudaMemcpy(dst, host_src, bytes, cudaMemcpyHostToDevice));
+    return GSPH_OK;
+}
+
+gsph_status gsph_copy_in_async(gsph_handle h, gsph_field field,
+                               const void *host_src, size_t bytes) {
+    gsph_status st = check_handle(h);
+    if (st) return st;
+    System &s = h->sys;
+    float4 *dst = state_ptr(s, field);
+    if (!dst || !host_src || bytes != size_t(s.n) * sizeof(float4)) {
+        set_error("gsph_copy_in_async: bad field, source or size");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    if (bytes)
+        GSPH_CUDA(cudaMemcpyAsync(dst, host_src, bytes, cudaMemcpyHostToDevice,
+                                  s.stream));
+    return GSPH_OK;
+}
+
+gsph_status gsph_copy_out_async(gsph_handle h, gsph_field field, void *host_dst,
+                                size_t bytes) {
+    gsph_status st = check_handle(h);
+    if (st) return st;
+    System &s = h->sys;
+    float4 *src = state_ptr(s, field);
+    if (!src || !host_dst || bytes != size_t(s.n) * sizeof(float4)) {
+        set_error("gsph_copy_out_async: bad field, destination or size");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    if (bytes)
+        GSPH_CUDA(cudaMemcpyAsync(host_dst, src, bytes, cudaMemcpyDeviceToHost,
+                                  s.stream));
+    return GSPH_OK;
+}
+
+gsph_status gsph_checksum(gsph_handle h, double out[5]) {
+    gsph_status st = check_handle(h);
+    if (st) return st;
+    System &s = h->sys;
+    launch_checksum(s.pos[s.cur], s.n, s.red, s.stream);
+    if ((st = s.check_launch())) return st;
+    GSPH_CUDA(cudaMemcpyAsync(out, s.red, 5 * sizeof(double),
+                              cudaMemcpyDeviceToHost, s.stream));
+    GSPH_CUDA(cudaStreamSynchronize(s.stream));
+    return GSPH_OK;
+}
+
+gsph_status gsph_reductions(gsph_handle h, double out[8]) {
+    gsph_status st = check_handle(h);
+    if (st) return st;
+    System &s = h->sys;
+    launch_reductions(s.pos[s.cur], s.vel[s.cur], s.n, s.params.mass, s.red,
+                      s.stream);
+    if ((st = s.check_launch())) return st;
+    GSPH_CUDA(cudaMemcpyAsync(out, s.red, 8 * sizeof(double),
+                              cudaMemcpyDeviceToHost, s.stream));
+    GSPH_CUDA(cudaStreamSynchronize(s.stream));
+    return GSPH_OK;
+}
+
+gsph_status gsph_set_stage_timing(gsph_handle h, int enabled) {
+    gsph_status st = check_handle(h);
+    if (st) return st;
+    h->sys.timing = enabled != 0;
+    return GSPH_OK;
+}
+
+gsph_status gsph_stage_times(gsph_handle h, float out[4]) {
+    gsph_status st = check_handle(h);
+    if (st) return st;
+    if (!out) {
+        set_error("gsph_stage_times: null output");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    return h->sys.stage_times(out);
+}
+
+gsph_status gsph_benchmark(gsph_handle h, int frames, gsph_bench_report *out) {
+    gsph_status st = check_handle(h);
+    if (st) return st;
+    if (!out || frames <= 0) {
+        set_error("gsph_benchmark: frame count must be positive");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    System &s = h->sys;
+    std::memset(out, 0, sizeof(*out));
+    // Warm-up frames with per-stage events (sph_hybrid_system.cpp:356-370).
+    const int warm = frames < 5 ? frames : 5;
+    const bool old_timing = s.timing;
+    float stage[4] = {0, 0, 0, 0};
+    s.timing = true;
+    {
+        float tmp[4];
+        s.stage_times(tmp);   // drop anything pending
+    }
+    for (int i = 0; i < warm; ++i)
+        if ((st = s.tick())) return st;
+    s.stage_times(stage);
+    s.timing = false;
+    const int measured = frames - warm;
+    GSPH_CUDA(cudaStreamSynchronize(s.stream));
+    const auto t0 = std::chrono::steady_clock::now();
+    for (int i = 0; i < measured; ++i)
+        if ((st = s.tick())) return st;
+    GSPH_CUDA(cudaStreamSynchronize(s.stream));
+    const auto t1 = std::chrono::steady_clock::now();
+    s.timing = old_timing;
+    const double elapsed = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    const double total_kernel = stage[0] + stage[1] + stage[2] + stage[3];
+    out->measured_frames = measured;
+    out->warmup_frames = warm;
+    out->total_wall_ms = elapsed;
+    out->avg_frame_ms = measured > 0 ? elapsed / measured : total_kernel;
+    out->fps = out->avg_frame_ms > 0 ? 1000.0 / out->avg_frame_ms : 0.0;
+    out->particle_steps_per_s =
+        out->avg_frame_ms > 0 ? double(s.n) * 1000.0 / out->avg_frame_ms : 0.0;
+    out->arrange_ms = stage[0];
+    out->density_ms = stage[1];
+    out->force_ms = stage[2];
+    out->integrate_ms = stage[3];
+    out->total_kernel_ms = total_kernel;
+    if ((st = gsph_checksum(h, out->checksum))) return st;
+    if ((st = s.sync_and_check())) return st;
+    Counters c;
+    if ((st = s.read_counters(c))) return st;
+    out->tra_particles = c.middle;
+    out->sms_tasks = c.task_count;
+    // Pair statistics (getSmsTaskPairStats, sph_arrangement.cu:1595-1636).
+    const int T = c.task_count;
+    if (T > 0) {
+        std::vector<gsph_block_task> tasks(size_t(T + (T & 1)));
+        GSPH_CUDA(cudaMemcpy(tasks.data(), s.fr.tasks,
+                             tasks.size() * sizeof(gsph_block_task),
+                             cudaMemcpyDeviceToHost));
+        out->total_pairs = (T + 1) / 2;
+        for (int i = 0; i < T; i += 2) {
+            const gsph_block_task &a = tasks[size_t(i)];
+            const gsph_block_task &b = tasks[size_t(i) + 1];
+            if (a.is_same) {
+                ++out->is_same_pairs;
+                if (a.cell_particle_count - int(b.p_offset) >= kSmsTaskParticles)
+                    ++out->full_is_same_pairs;
+                else
+                    ++out->partial_is_same_pairs;
+                if (a.xxi == b.xxx)
+                    ++out->compact_is_same_pairs;
+                else
+                    ++out->widened_is_same_pairs;
+            }
+            if (a.cellid == b.cellid) ++out->same_cell_pairs;
+        }
+    }
+    return GSPH_OK;
+}
+
+// ------------------------------------------------------- kernel-level API --
+size_t gsph_grid_sort_scratch_bytes(uint32_t n, uint32_t numc) {
+    const size_t N = std::max<size_t>(n, 1), C = std::max<size_t>(numc, 1);
+    const size_t occ = std::max<size_t>(std::min(N, C), 1);
+    const size_t tiles = (C + kScanTile - 1) / kScanTile;
+    size_t b = 0;
+    b += align_up(N * 4, 256);      // key_in
+    b += align_up(N * 4, 256);      // slot
+    b += align_up(N * 8, 256);      // pairs
+    b += align_up(C * 4, 256);      // cell_count
+    b += align_up(C * 4, 256);      // cell_xslab
+    b += align_up(occ * 4, 256);    // occ_list
+    b += align_up(occ * 4, 256);    // big_list
+    b += align_up(tiles * 8, 256);  // scan tiles
+    b += align_up(sizeof(Counters), 256);
+    return b;
+}
+
+gsph_status gsph_grid_sort_dev(const gsph_params *p, uint32_t n,
+                               const float *pos_in, const float *vel_in,
+                               const float *ev_in, float *pos_out,
+                               float *vel_out, float *ev_out, uint32_t *key_out,
+                               int32_t *perm_out, int32_t *cell_start_out,
+                               void *scratch, size_t scratch_bytes,
+                               void *stream) {
+    if (!p || !pos_in || !vel_in || !ev_in || !pos_out || !vel_out || !ev_out ||
+        !key_out || !perm_out || !cell_start_out || !scratch) {
+        set_error("gsph_grid_sort_dev: null argument");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    const DevParams dp = make_dev_params(*p);
+    if (dp.numc <= 0 || n > 0x7FFFFFFFu) {
+        set_error("gsph_grid_sort_dev: empty grid or too many particles");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    const size_t need = gsph_grid_sort_scratch_bytes(n, uint32_t(dp.numc));
+    if (scratch_bytes < need) {
+        set_error("gsph_grid_sort_dev: scratch of %zu bytes, %zu needed",
+                  scratch_bytes, need);
+        return GSPH_ERR_INVALID_ARG;
+    }
+    if (reinterpret_cast<uintptr_t>(scratch) % 256 != 0) {
+        set_error("gsph_grid_sort_dev: scratch must be 256-byte aligned");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    int dev = 0;
+    GSPH_CUDA(cudaGetDevice(&dev));
+    const size_t N = std::max<size_t>(n, 1), C = size_t(dp.numc);
+    const size_t occ = std::max<size_t>(std::min(N, C), 1);
+    const size_t tiles = (C + kScanTile - 1) / kScanTile;
+    char *w = static_cast<char *>(scratch);
+    auto carve = [&](size_t bytes) {
+        char *r = w;
+        w += align_up(bytes, 256);
+        return r;
+    };
+    Frame f{};
+    f.n = int(n);
+    f.pos_in = reinterpret_cast<const float4 *>(pos_in);
+    f.vel_in = reinterpret_cast<const float4 *>(vel_in);
+    f.ev_in = reinterpret_cast<const float4 *>(ev_in);
+    f.pos = reinterpret_cast<float4 *>(pos_out);
+    f.vel = reinterpret_cast<float4 *>(vel_out);
+    f.ev = reinterpret_cast<float4 *>(ev_out);
+    f.key = key_out;
+    f.perm = perm_out;
+    f.cell_start = cell_start_out;
+    f.key_in = reinterpret_cast<uint32_t *>(carve(N * 4));
+    f.slot = reinterpret_cast<uint32_t *>(carve(N * 4));
+    f.pairs = reinterpret_cast<unsigned long long *>(carve(N * 8));
+    f.cell_count = reinterpret_cast<int32_t *>(carve(C * 4));
+    f.cell_xslab = reinterpret_cast<uint32_t *>(carve(C * 4));
+    f.occ_list = reinterpret_cast<int32_t *>(carve(occ * 4));
+    f.big_list = reinterpret_cast<int32_t *>(carve(occ * 4));
+    f.scan_tiles = reinterpret_cast<unsigned long long *>(carve(tiles * 8));
+    f.ctr = reinterpret_cast<Counters *>(carve(sizeof(Counters)));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    GSPH_CUDA(cudaMemsetAsync(f.cell_count, 0, C * 4, s));
+    GSPH_CUDA(cudaMemsetAsync(f.ctr, 0, sizeof(Counters), s));
+    launch_hash_count(f, dp, s);
+    launch_cell_scan(f, dp, s);
+    launch_scatter_pairs(f, s);
+    launch_cell_sort(f, device_sm_count(dev), s);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error("gsph_grid_sort_dev: launch failed: %s", cudaGetErrorString(e));
+        return GSPH_ERR_CUDA;
+    }
+    return GSPH_OK;
+}
+
+}  // extern "C"

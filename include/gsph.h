@@ -1,0 +1,248 @@
+/*
+ * gsph.h — C ABI of the GB300-native weakly-compressible SPH step.
+ *
+ * This is the drop-in boundary for the reference's single-scene hot path
+ * (KemengHuang/Fast-General-GPU-SPH-framework). Every entry point below names
+ * the reference interface it replaces (path:line in that project):
+ *
+ *   reference                                   here
+ *   -----------------------------------------   -------------------------------
+ *   readSceneFromJsonFile  sph_hybrid_system.cpp:69-126      gsph_scene_load_json
+ *   defaultInitializeSPHSysPara  sph_hybrid_system.cpp:127-202 gsph_params_init
+ *   initializeScene lattice  sph_hybrid_system.cpp:432-473   gsph_lattice_count/fill
+ *   HybridSystem ctor  sph_hybrid_system.cpp:209-240          gsph_create*
+ *   HybridSystem::tick  sph_hybrid_system.cpp:253-339         gsph_step
+ *   Arrangement::arrangeHybridFrame  sph_arrangement.cu:1493  gsph_arrange
+ *   computeDensityHybrid  kernel_dispatch.cu:206-222          gsph_density
+ *   computeForceHybrid  kernel_dispatch.cu:224-253            gsph_force
+ *   advance  kernel_dispatch.cu:314-323                       gsph_advance
+ *   HybridSystem::runBenchmark  sph_hybrid_system.cpp:341-430 gsph_benchmark
+ *   computeBenchmarkStateChecksum  sph_hybrid_system.cpp:43-62 gsph_checksum
+ *   getNumParticles / getPosition  sph_hybrid_system.h        gsph_get_info / gsph_copy_out
+ *   Arrangement getters  sph_arrangement.h:41-59              gsph_copy_out fields
+ *
+ * Conventions: every function returns gsph_status (0 = success, negative =
+ * error) and never exits the process; gsph_last_error() returns the message of
+ * the calling thread's last failure. A handle owns its device memory and one
+ * CUDA stream; all work is asynchronous on that stream until a call that
+ * returns host data (copy_out, checksum, benchmark, sync). A handle may be used
+ * from one thread at a time; different handles are independent (parameters
+ * live in each handle, not in a process-global constant bank).
+ * There is no CPU fallback: without a usable CUDA device, creation fails with
+ * GSPH_ERR_NO_DEVICE.
+ */
+#ifndef GSPH_H_
+#define GSPH_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GSPH_ABI_VERSION 1
+#define GSPH_MAX_FLUID_BLOCKS 64
+
+typedef int gsph_status;
+enum {
+    GSPH_OK = 0,
+    GSPH_ERR_INVALID_ARG = -1,
+    GSPH_ERR_IO = -2,
+    GSPH_ERR_PARSE = -3,
+    GSPH_ERR_CUDA = -4,
+    GSPH_ERR_OUT_OF_MEMORY = -5,
+    GSPH_ERR_CAPACITY = -6,
+    GSPH_ERR_DOMAIN = -7,     /* a particle left the grid (device flag) */
+    GSPH_ERR_NO_DEVICE = -8,
+    GSPH_ERR_STATE = -9
+};
+
+typedef struct gsph_system *gsph_handle;
+
+/* Scene file contents (reference Scene, sph_hybrid_system.h:37-44, and the
+ * JSON keys read at sph_hybrid_system.cpp:83-117). Defaults as in the
+ * reference: interval 0.5, mass 0.02, recomm_nump 65536, box 0. */
+typedef struct {
+    float world[3];                 /* "xx","yy","zz" */
+    float mass;                     /* "mass" */
+    float interval;                 /* "interval" (lattice step / h) */
+    uint32_t recomm_nump;           /* "recomm_nump" */
+    uint32_t n_blocks;              /* "fluid_block" entries */
+    float block_begin[GSPH_MAX_FLUID_BLOCKS][3];
+    float block_end[GSPH_MAX_FLUID_BLOCKS][3];
+    /* Optional physics keys (not in the reference's files; absent = NaN,
+     * meaning "use the reference's hard-coded value"). */
+    float kernel;                   /* "kernel" (h) */
+    float rest_density;             /* "rest_density" */
+    float gas_constant;             /* "gas_constant" */
+    float viscosity;                /* "viscosity" */
+    float time_step;                /* "time_step" */
+    float gravity_y;                /* "gravity_y" */
+    float jitter;                   /* "jitter" (fraction of lattice step) */
+    uint64_t seed;                  /* "seed" */
+} gsph_scene;
+
+/* Physical parameters, the live subset of the reference SystemParameter
+ * (core/sph_parameter.h:18-90) with its derived coefficients. */
+typedef struct {
+    float world_size[3];
+    float cell_size, inv_cell_size;
+    int32_t grid_size[3];
+    float kernel, kernel_2, mass;
+    float gravity[3];
+    float wall_damping, rest_density, gas_constant, viscosity, time_step;
+    float surface_normal, surface_coe;
+    float poly6_value, spiky_value, visco_value, grad_poly6, lplc_poly6;
+    float self_density;
+    float inv_rest_density, density_scale, half_spiky_value;
+    float viscosity_visco_value, grad_color_scale, lplc_color_scale;
+    float bound_interval, bound_min[3], bound_max[3];
+} gsph_params;
+
+/* BlockTask, the reference's 32-byte SMS task descriptor
+ * (particle/particle_buffer.h:60-87), same field layout. */
+typedef struct {
+    int8_t is_same;
+    uint8_t pad_;
+    uint16_t paired_bounds;
+    int32_t cellid;
+    uint16_t cell_pos[3];
+    uint16_t p_offset;
+    int8_t xxi, xxx, yyi, yyy, zzi, zzz;
+    int32_t cell_begin;
+    int32_t cell_particle_count;
+} gsph_block_task;
+
+typedef struct {
+    uint32_t n_particles;
+    uint32_t n_cells;            /* numc = gx*gy*gz */
+    int32_t grid_size[3];
+    int32_t tra_particles;       /* "middle" after the last arrange */
+    int32_t sms_tasks;           /* SMS task count after the last arrange */
+    int32_t occupied_cells;
+    int32_t big_cells;           /* cells sorted by the block-level path */
+    uint64_t frames;             /* ticks executed */
+    uint64_t device_bytes;       /* device memory held by the handle */
+} gsph_info;
+
+/* Report of gsph_benchmark (the print block of runBenchmark,
+ * sph_hybrid_system.cpp:397-429). */
+typedef struct {
+    int32_t measured_frames, warmup_frames;
+    double total_wall_ms, avg_frame_ms, fps;
+    double checksum[5];          /* x, y, z, 1/rho, weighted */
+    int32_t tra_particles, sms_tasks;
+    int32_t is_same_pairs, total_pairs, same_cell_pairs;
+    int32_t full_is_same_pairs, partial_is_same_pairs;
+    int32_t compact_is_same_pairs, widened_is_same_pairs;
+    double arrange_ms, density_ms, force_ms, integrate_ms, total_kernel_ms;
+    double particle_steps_per_s;
+} gsph_bench_report;
+
+/* Fields for gsph_copy_out / gsph_copy_in. All particle fields are in the
+ * handle's current (sorted) order. */
+typedef enum {
+    GSPH_FIELD_POSITION = 0,      /* float4[N]  x,y,z, w = 1/rho             */
+    GSPH_FIELD_VELOCITY = 1,      /* float4[N]  x,y,z, w unused             */
+    GSPH_FIELD_EVAL_VELOCITY = 2, /* float4[N]  x,y,z, w = pressure          */
+    GSPH_FIELD_ACCELERATION = 3,  /* float4[N]  force/acceleration, w unused */
+    GSPH_FIELD_KEY = 4,           /* uint32[N]  sorted micro-cell key        */
+    GSPH_FIELD_PERMUTATION = 5,   /* int32[N]   source index of each slot    */
+    GSPH_FIELD_CELL_START = 6,    /* int32[numc+1] coarse cell offsets       */
+    GSPH_FIELD_CELL_COUNT = 7,    /* int32[numc] coarse cell counts          */
+    GSPH_FIELD_MICRO_START = 8,   /* int32[numc*64+1] dense micro offsets    */
+    GSPH_FIELD_BLOCK_REQ = 9,     /* int32[numc] SMS tasks per cell          */
+    GSPH_FIELD_COMPACT_INDEX = 10,/* int32[N] TRA particles then SMS ones    */
+    GSPH_FIELD_TASKS = 11,        /* gsph_block_task[T + (T&1)]              */
+    GSPH_FIELD_SPLIT = 12         /* int32[2] {middle, task count}           */
+} gsph_field;
+
+const char *gsph_last_error(void);
+int gsph_abi_version(void);
+
+/* Scene + parameters + initial lattice (host-side; no device needed). */
+gsph_status gsph_scene_default(gsph_scene *out);
+gsph_status gsph_scene_load_json(const char *path, gsph_scene *out);
+gsph_status gsph_scene_parse_json(const char *text, size_t len, gsph_scene *out);
+gsph_status gsph_params_init(const gsph_scene *scene, gsph_params *out);
+gsph_status gsph_lattice_count(const gsph_scene *scene, const gsph_params *p,
+                               uint32_t *count);
+/* Writes count float4 positions (w = 0), in the reference's x -> y -> z loop
+ * order with FP32 accumulation; applies the scene's seeded jitter if any. */
+gsph_status gsph_lattice_fill(const gsph_scene *scene, const gsph_params *p,
+                              float *pos4, uint32_t capacity, uint32_t *count);
+
+/* Lifetime. pos4/vel4 are host float4 arrays (vel4 may be NULL: zero). */
+gsph_status gsph_create(const gsph_params *p, const float *pos4,
+                        const float *vel4, uint32_t n, int device,
+                        gsph_handle *out);
+gsph_status gsph_create_from_json(const char *scene_path, int device,
+                                  gsph_handle *out);
+gsph_status gsph_destroy(gsph_handle h);
+
+/* One frame = arrange + density + force + advance (tick). */
+gsph_status gsph_step(gsph_handle h, int n_steps);
+gsph_status gsph_arrange(gsph_handle h);
+gsph_status gsph_density(gsph_handle h);
+gsph_status gsph_force(gsph_handle h);
+gsph_status gsph_advance(gsph_handle h);
+/* Capture whole frames in CUDA graphs (1) or launch stage by stage (0). */
+gsph_status gsph_set_graph_mode(gsph_handle h, int enabled);
+gsph_status gsph_sync(gsph_handle h);
+/* The handle's CUDA stream (a cudaStream_t), for callers that order their own
+ * work or timing events against the handle's kernels. */
+gsph_status gsph_stream(gsph_handle h, void **stream_out);
+
+gsph_status gsph_get_info(gsph_handle h, gsph_info *out);
+gsph_status gsph_get_params(gsph_handle h, gsph_params *out);
+gsph_status gsph_copy_out(gsph_handle h, gsph_field field, void *host_dst,
+                          size_t bytes);
+/* Overwrites particle state (POSITION, VELOCITY, EVAL_VELOCITY,
+ * ACCELERATION only) in the current order. */
+gsph_status gsph_copy_in(gsph_handle h, gsph_field field, const void *host_src,
+                         size_t bytes);
+/* Asynchronous pinned-host copies on the handle's stream (host buffers must
+ * stay valid until the next gsph_sync). */
+gsph_status gsph_copy_in_async(gsph_handle h, gsph_field field,
+                               const void *host_src, size_t bytes);
+gsph_status gsph_copy_out_async(gsph_handle h, gsph_field field,
+                                void *host_dst, size_t bytes);
+
+/* FP64 state checksum as the reference's benchmark prints it:
+ * {sum x, sum y, sum z, sum w, sum ((i&1023)+1)*(x+3y+7z)}. */
+gsph_status gsph_checksum(gsph_handle h, double out[5]);
+/* Order-independent FP64 reductions on the device: {sum m, sum m*v.x, .y, .z,
+ * kinetic energy, sum x, sum y, sum z}. */
+gsph_status gsph_reductions(gsph_handle h, double out[8]);
+
+gsph_status gsph_benchmark(gsph_handle h, int frames, gsph_bench_report *out);
+/* Stage timing: while enabled, every frame records CUDA events on the
+ * handle's stream between its stages (frames then run without graphs).
+ * gsph_stage_times waits for the stream and returns the mean device time (ms)
+ * per frame since the previous call: {arrange, density, force, integrate};
+ * density and force are one kernel launch each. */
+gsph_status gsph_set_stage_timing(gsph_handle h, int enabled);
+gsph_status gsph_stage_times(gsph_handle h, float out[4]);
+
+/* Kernel-level entry: the grid sort (arrange stage, A2-A5) over caller-owned
+ * device buffers (the Arrangement path, sph_arrangement.cu:1352-1395).
+ * Positions/velocities/evaluated velocities are float4 device arrays of n
+ * particles; the sorted copies go to the *_out arrays; key_out (uint32[n]),
+ * perm_out (int32[n]) and cell_start_out (int32[numc+1]) receive the grid.
+ * scratch/scratch_bytes is caller-owned device memory of at least
+ * gsph_grid_sort_scratch_bytes(n, numc) bytes. stream is a cudaStream_t. */
+size_t gsph_grid_sort_scratch_bytes(uint32_t n, uint32_t numc);
+gsph_status gsph_grid_sort_dev(const gsph_params *p, uint32_t n,
+                               const float *pos_in, const float *vel_in,
+                               const float *ev_in, float *pos_out,
+                               float *vel_out, float *ev_out,
+                               uint32_t *key_out, int32_t *perm_out,
+                               int32_t *cell_start_out, void *scratch,
+                               size_t scratch_bytes, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GSPH_H_ */

@@ -1,0 +1,58 @@
+"""The C-ABI library loads and exports every function include/gsph.h declares
+(no compute call: this runs without a GPU)."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def declared_functions():
+    text = (ROOT / "include" / "gsph.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"\b(gsph_\w+)\s*\(", text)
+    return sorted(set(n for n in names if not n.endswith("_t")))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for required in ["gsph_create", "gsph_step", "gsph_arrange", "gsph_density",
+                     "gsph_force", "gsph_advance", "gsph_benchmark", "gsph_copy_out",
+                     "gsph_scene_load_json", "gsph_grid_sort_dev"]:
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol(gsph):
+    lib = C.CDLL(str(gsph.LIB_PATH))
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header(gsph):
+    assert set(declared_functions()) <= set(gsph._SIGS)
+
+
+def test_struct_sizes(gsph):
+    assert C.sizeof(gsph.BlockTask) == 32
+    assert gsph.load_library().gsph_abi_version() == 1
+
+
+def test_scratch_size_query(gsph):
+    lib = gsph.load_library()
+    small = lib.gsph_grid_sort_scratch_bytes(1000, 4096)
+    big = lib.gsph_grid_sort_scratch_bytes(1 << 20, 1 << 20)
+    assert 0 < small < big
+    assert small % 256 == 0
+
+
+def test_create_without_device_fails_cleanly(gsph):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    s = gsph.load_scene(gsph.scene_path("dam_break_262k.json"))
+    with pytest.raises(gsph.GsphError) as ei:
+        gsph.HybridSystem(gsph.scene_path("dam_break_262k.json"))
+    assert ei.value.status == gsph.ERR_NO_DEVICE
+    assert s.n_blocks == 1
