@@ -382,7 +382,7 @@ static void density_d(const double *pos4, const uint32_t *key_sorted,
 /* FP64 force core on double state (pos w = 1/rho, ev w = pressure). */
 static void force_d(const double *pos4, const double *ev4,
                     const uint32_t *key_sorted, const int32_t *cell_start,
-                    long n, const gsph_params *p, double *acc3) {
+                    long n, const gsph_params *p, double *acc3, double *mag) {
     const int gx = p->grid_size[0], gy = p->grid_size[1], gz = p->grid_size[2];
     const double h = (double)p->kernel, h2 = h * h;
 #pragma omp parallel for schedule(dynamic, 1024)
@@ -394,6 +394,7 @@ static void force_d(const double *pos4, const double *ev4,
         const double vxi = ev4[4 * i], vyi = ev4[4 * i + 1], vzi = ev4[4 * i + 2],
                      pi = ev4[4 * i + 3];
         double P[3] = {0, 0, 0}, Vs[3] = {0, 0, 0}, G[3] = {0, 0, 0}, L = 0.0;
+        double Pm = 0.0, Vm = 0.0;   /* sums of |pair term| (conditioning) */
         for (int dz = -1; dz <= 1; ++dz)
             for (int dy = -1; dy <= 1; ++dy)
                 for (int dx = -1; dx <= 1; ++dx) {
@@ -412,10 +413,15 @@ static void force_d(const double *pos4, const double *ev4,
                         P[0] -= rx * pw;
                         P[1] -= ry * pw;
                         P[2] -= rz * pw;
+                        Pm += fabs(pw) * d;
                         const double wk = V * k;
-                        Vs[0] += (ev4[4 * j] - vxi) * wk;
-                        Vs[1] += (ev4[4 * j + 1] - vyi) * wk;
-                        Vs[2] += (ev4[4 * j + 2] - vzi) * wk;
+                        const double ux = (ev4[4 * j] - vxi) * wk;
+                        const double uy = (ev4[4 * j + 1] - vyi) * wk;
+                        const double uz = (ev4[4 * j + 2] - vzi) * wk;
+                        Vs[0] += ux;
+                        Vs[1] += uy;
+                        Vs[2] += uz;
+                        Vm += sqrt(ux * ux + uy * uy + uz * uz);
                         const double hr = h2 - d2;
                         const double gw = V * hr * hr;
                         G[0] += rx * gw;
@@ -438,6 +444,10 @@ static void force_d(const double *pos4, const double *ev4,
                 sf = G[a] * (double)p->surface_coe * L / nrm;
             acc3[3 * i + a] = F[a] + sf;
         }
+        if (mag)
+            mag[i] = (Pm * fabs((double)p->half_spiky_value) +
+                      Vm * fabs((double)p->viscosity_visco_value)) *
+                     (double)p->mass;
     }
 }
 
@@ -465,18 +475,21 @@ ORACLE_EXPORT int oracle_density(const float *pos4, const uint32_t *key_sorted,
 
 /* Force of every sorted particle (FP64) from single-precision inputs with
  * pos4.w = 1/rho and ev4.w = pressure as the density pass stores them.
- * Output acc3[3n]. */
+ * Output acc3[3n]; mag[n] (may be NULL) receives the sum over pairs of the
+ * magnitude of each pressure and viscosity pair term, i.e. the scale of the
+ * rounding error of any summation of those terms. */
 ORACLE_EXPORT int oracle_force(const float *pos4, const float *ev4,
                                const uint32_t *key_sorted,
                                const int32_t *cell_start, long n,
-                               const gsph_params *p, double *acc3) {
+                               const gsph_params *p, double *acc3,
+                               double *mag) {
     double *pd = widen(pos4, 4 * n), *ed = widen(ev4, 4 * n);
     if (!pd || !ed) {
         free(pd);
         free(ed);
         return -2;
     }
-    force_d(pd, ed, key_sorted, cell_start, n, p, acc3);
+    force_d(pd, ed, key_sorted, cell_start, n, p, acc3, mag);
     free(pd);
     free(ed);
     return 0;
@@ -574,7 +587,7 @@ ORACLE_EXPORT int oracle_step(double *pos4, double *vel4, double *ev4, long n,
         pos4[4 * i + 3] = 1.0 / rho[i];
         ev4[4 * i + 3] = rho[n + i];
     }
-    force_d(pos4, ev4, ks, cs, n, p, acc);
+    force_d(pos4, ev4, ks, cs, n, p, acc, NULL);
     oracle_integrate(pos4, vel4, ev4, acc, n, p);
     free(pf); free(ks); free(perm); free(cs); free(tmp); free(rho); free(acc);
     return bad;

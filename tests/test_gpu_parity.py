@@ -2,8 +2,13 @@
 
 Integer stages (keys, permutation, cell offsets, split, tasks) must be
 bit-exact. Physics is compared with the FP64 oracle on a common input state:
-density |d rho| / rho <= 1e-5; force |dF| / max(|F|, 1e-3 rms|F|) <= 1e-4;
-integrated positions within 1e-6 of the box size.
+  density   |d rho| / rho <= 1e-5
+  force     |dF| <= 1e-4 max(|F|, 1e-3 rms|F|) + 64 u S, where S is the sum of
+            the magnitudes of the particle's pair terms and u = 2^-24: any
+            FP32 summation of those terms carries an error of order u S, which
+            dominates where pressure pairs cancel (about 1,200 neighbours in
+            the dense scene)
+  integrate positions within 1e-6 of the box size.
 """
 import numpy as np
 import pytest
@@ -14,6 +19,7 @@ pytestmark = pytest.mark.gpu
 
 RHO_TOL = 1e-5
 FORCE_TOL = 1e-4
+FORCE_SUM_TOL = 64 * 2.0 ** -24
 POS_TOL = 1e-6
 
 
@@ -125,11 +131,14 @@ def test_force_vs_fp64(gsph, oracle, scene):
         acc = sysm.copy_out(gsph.FIELD_ACCELERATION)[:, :3].astype(np.float64)
         ks = sysm.copy_out(gsph.FIELD_KEY)
         cs = sysm.copy_out(gsph.FIELD_CELL_START)
-    ref = oracle.force(spos, sev, ks, cs, p)
+    ref, mag = oracle.force(spos, sev, ks, cs, p, with_mag=True)
     fn = np.linalg.norm(ref, axis=1)
     floor = 1e-3 * np.sqrt(np.mean(fn ** 2))
-    err = np.linalg.norm(acc - ref, axis=1) / np.maximum(fn, floor)
-    assert err.max() <= FORCE_TOL, (name, err.max())
+    bound = FORCE_TOL * np.maximum(fn, floor) + FORCE_SUM_TOL * mag
+    dev = np.linalg.norm(acc - ref, axis=1)
+    assert np.all(dev <= bound), (name, (dev / bound).max())
+    # the bulk is far tighter than the bound
+    assert np.median(dev / np.maximum(fn, floor)) <= 1e-5, name
 
 
 def test_integrate_vs_fp64(gsph, oracle, scene):
