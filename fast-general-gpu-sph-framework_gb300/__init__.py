@@ -189,6 +189,8 @@ _SIGS = {
     "gsph_grid_sort_scratch_bytes": ([C.c_uint32, C.c_uint32], C.c_size_t),
     "gsph_grid_sort_dev": ([C.POINTER(Params), C.c_uint32, _VP, _VP, _VP, _VP, _VP, _VP,
                             _VP, _VP, _VP, _VP, C.c_size_t, _VP], C.c_int),
+    "gsph_grid_sort_dev_noalloc": ([C.POINTER(Params), C.c_uint32, _VP, _VP, _VP, _VP, _VP,
+                                    _VP, _VP, _VP, _VP, _VP], C.c_int),
 }
 
 _lib = None

@@ -19,7 +19,7 @@ CSRC = PKG / "csrc"
 LIB = PKG / "lib"
 ROOT = PKG.parent
 
-CUDA_SOURCES = ["grid.cu", "split.cu", "physics.cu", "system.cu"]
+CUDA_SOURCES = ["grid.cu", "split.cu", "physics.cu", "system.cu", "noalloc.cu"]
 CXX_SOURCES = ["scene.cpp"]
 GENCODE = "arch=compute_103a,code=sm_103a"
 

@@ -241,6 +241,31 @@ gsph_status gsph_grid_sort_dev(const gsph_params *p, uint32_t n,
                                int32_t *cell_start_out, void *scratch,
                                size_t scratch_bytes, void *stream);
 
+/* The same grid sort for callers that cannot allocate device memory at the
+ * call site: hosts that run under a fixed device-memory budget kept by their
+ * own pool allocator (a raw cudaMalloc would fail or escape the budget), and
+ * real-time loops that cannot pay cudaMalloc's implicit synchronisation.
+ * No counterpart in the reference: it is an addition of this library.
+ * The caller passes inputs and outputs only; the scratch is a fixed
+ * file-scope device array of GSPH_NOALLOC_SCRATCH_BYTES that every GPU which
+ * loads the library holds until the process exits. Limits: at most
+ * GSPH_NOALLOC_MAX_PARTICLES particles and GSPH_NOALLOC_MAX_CELLS cells;
+ * larger inputs return GSPH_ERR_CAPACITY without launching anything. The
+ * first call on a device looks up the array's device address on that device
+ * (make that first call before any stream capture). Calls share the array:
+ * each call clears what it accumulates into, but calls that overlap on the
+ * GPU (different streams, or different host threads) race. Allocates
+ * nothing: no cudaMalloc, cudaFree or allocating library routine. */
+#define GSPH_NOALLOC_MAX_PARTICLES 262144u
+#define GSPH_NOALLOC_MAX_CELLS 524288u
+#define GSPH_NOALLOC_SCRATCH_BYTES 10487040u
+gsph_status gsph_grid_sort_dev_noalloc(const gsph_params *p, uint32_t n,
+                                       const float *pos_in, const float *vel_in,
+                                       const float *ev_in, float *pos_out,
+                                       float *vel_out, float *ev_out,
+                                       uint32_t *key_out, int32_t *perm_out,
+                                       int32_t *cell_start_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
