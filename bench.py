@@ -228,6 +228,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true",
+                    help="skip the end-to-end loop (profiling runs)")
     ap.add_argument("--scene", default=SCENE)
     args = ap.parse_args()
     ws, rank, local = dist_env()
@@ -295,7 +297,7 @@ def main():
     for h, f in zip(host, fields):
         sysm.copy_out_async(f, h.data_ptr(), h.numel() * 4)
     sysm.sync()
-    e2e_steps = max(3, min(args.steps, 20))
+    e2e_steps = 0 if args.no_e2e else max(3, min(args.steps, 20))
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -312,7 +314,7 @@ def main():
         t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
-    e2e_value = ws * n * e2e_steps / e2e_s
+    e2e_value = ws * n * e2e_steps / e2e_s if e2e_steps else None
     state_bytes = 3 * n * 16
 
     cpu = None
