@@ -26,6 +26,12 @@ constexpr int kBigCellSmem = 4096;
 constexpr int kSmsTaskParticles = 32;
 // Sentinel for cell_xslab: slab boundaries unknown, search the whole cell.
 constexpr uint32_t kXslabUnknown = 0xFFFFFFFFu;
+// Neighbour masks of TRA particles: the density pass records, for each of the
+// 9 neighbour rows of a TRA particle, a 32-bit mask of which candidates of the
+// row interact; the force pass walks the set bits instead of re-testing every
+// candidate. A particle with a row longer than 32 candidates is flagged and
+// the force pass scans its candidates instead.
+constexpr int kMaskRowMax = 32;
 // Scan tile (items per CTA) for the reduce-then-scan kernels.
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;
@@ -82,6 +88,12 @@ struct Frame {
     gsph_block_task *tasks;
     int32_t task_capacity;
     int32_t *compact;
+    // TRA neighbour masks, interleaved by 32-particle chunk of the compact
+    // index: row r of compact index i at nbr_mask[((i >> 5) * 9 + r) * 32 +
+    // (i & 31)]; nbr_flag[i] = number of neighbours, or -1 where the masks
+    // are incomplete.
+    uint32_t *nbr_mask;
+    int32_t *nbr_flag;
     unsigned long long *scan_tiles;            // tile sums, cell scan
     int4 *scan_tiles4;                         // tile sums, task scan
     Counters *ctr;
@@ -98,7 +110,9 @@ void launch_split(const Frame &f, const DevParams &P, int max_occ,
 // ---- launchers (physics.cu) ----
 void launch_density(const Frame &f, const DevParams &P, int num_sms,
                     cudaStream_t s);
-void launch_force(const Frame &f, const DevParams &P, int num_sms,
+// fresh: the density pass ran on the current state, so the TRA neighbour
+// masks are valid.
+void launch_force(const Frame &f, const DevParams &P, int num_sms, bool fresh,
                   cudaStream_t s);
 void launch_integrate(const Frame &f, const DevParams &P, cudaStream_t s);
 void launch_reductions(const float4 *pos, const float4 *vel, int n,

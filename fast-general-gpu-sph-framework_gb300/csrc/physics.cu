@@ -183,7 +183,7 @@ __device__ __forceinline__ void write_force(const Frame &f, const DevParams &P,
 constexpr int kWarpsPerBlock = 8;
 
 // ---------------------------------------------------------------- density --
-__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 6)
 k_density(Frame f, DevParams P) {
     __shared__ float4 stage[kWarpsPerBlock][32];
     const int lane = threadIdx.x & 31;
@@ -198,23 +198,43 @@ k_density(Frame f, DevParams P) {
         u = __shfl_sync(kFull, u, 0);
         if (u >= total) break;
         if (u < tra_units) {
-            // TRA: one particle per lane (density_kernels.cu:318-366).
+            // TRA: one particle per lane (density_kernels.cu:318-366). Which
+            // candidates of each row interact is also recorded as a bit mask
+            // for the force pass.
             const int idx = (u << 5) + lane;
             if (idx >= middle) continue;
             const int self = f.compact[idx];
             const float4 p = f.pos[self];
             const MicroPos mp = micro_of(p, P);
+            uint32_t *masks = f.nbr_mask + size_t(u) * 9 * 32 + lane;
+            int incomplete = 0;
+            int found = 0;
             float sum = 0.f;
             for (int r = 0; r < 9; ++r) {
                 const int ny = mp.cy + (r % 3) - 1;
                 const int nz = mp.cz + (r / 3) - 1;
-                if (ny < 0 || ny >= P.gy || nz < 0 || nz >= P.gz) continue;
-                const int m = mp.cx + P.gx * (ny + P.gy * nz);
-                int begin, end;
-                row_range(f, P, m, mp.cx, mp.lmx, mp.lmx, begin, end);
-                for (int j = begin; j < end; ++j)
-                    sum += density_pair(p, f.pos[j], P.h2);
+                uint32_t mask = 0u;
+                if (ny >= 0 && ny < P.gy && nz >= 0 && nz < P.gz) {
+                    const int m = mp.cx + P.gx * (ny + P.gy * nz);
+                    int begin, end;
+                    row_range(f, P, m, mp.cx, mp.lmx, mp.lmx, begin, end);
+                    incomplete |= (end - begin > kMaskRowMax);
+                    uint32_t bit = 1u;
+#pragma unroll 4
+                    for (int j = begin; j < end; ++j, bit <<= 1) {
+                        const float4 q = f.pos[j];
+                        const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+                        const float d2 = dx * dx + dy * dy + dz * dz;
+                        if (P.h2 < d2 || kFloatSmall > d2) continue;
+                        const float t = P.h2 - d2;
+                        sum += t * t * t;
+                        mask |= bit;
+                    }
+                }
+                masks[r * 32] = mask;
+                found += __popc(mask);
             }
+            f.nbr_flag[idx] = incomplete ? -1 : found;
             write_density(f, P, self, sum, false);
         } else {
             // SMS: one 32-particle task per warp (density_kernels.cu:368-565).
@@ -250,10 +270,12 @@ k_density(Frame f, DevParams P) {
 }
 
 // ------------------------------------------------------------------ force --
-__global__ void __launch_bounds__(kWarpsPerBlock * 32)
-k_force(Frame f, DevParams P) {
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
+k_force(Frame f, DevParams P, bool fresh) {
     __shared__ float4 stage_p[kWarpsPerBlock][32];
     __shared__ float4 stage_v[kWarpsPerBlock][32];
+    __shared__ uint32_t row_mask[9][kWarpsPerBlock * 32];
+    __shared__ int row_start[9][kWarpsPerBlock * 32];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int middle = f.ctr->middle;
@@ -273,19 +295,55 @@ k_force(Frame f, DevParams P) {
             const float4 p = f.pos[self];
             const float4 pev = f.ev[self];
             const MicroPos mp = micro_of(p, P);
-            for (int r = 0; r < 9; ++r) {
-                const int ny = mp.cy + (r % 3) - 1;
-                const int nz = mp.cz + (r / 3) - 1;
-                if (ny < 0 || ny >= P.gy || nz < 0 || nz >= P.gz) continue;
-                const int m = mp.cx + P.gx * (ny + P.gy * nz);
-                int begin, end;
-                row_range(f, P, m, mp.cx, mp.lmx, mp.lmx, begin, end);
-                for (int j = begin; j < end; ++j) {
-                    const float4 q = f.pos[j];
-                    const float rx = p.x - q.x, ry = p.y - q.y, rz = p.z - q.z;
-                    const float d2 = rx * rx + ry * ry + rz * rz;
-                    if (P.h2 < d2 || kFloatSmall > d2) continue;
-                    force_pair(p, pev, q, f.ev[j], P, a);
+            const int found = fresh ? f.nbr_flag[idx] : -1;
+            if (found >= 0) {
+                // The neighbours the density pass found, in the same order:
+                // rows in sequence, set bits in increasing candidate index.
+                // Each lane stages its 9 (row start, mask) pairs in shared
+                // memory and walks all its neighbours in one loop, so lanes
+                // stay converged across rows.
+                const uint32_t *masks = f.nbr_mask + size_t(u) * 9 * 32 + lane;
+                for (int r = 0; r < 9; ++r) {
+                    const uint32_t mask = masks[r * 32];
+                    row_mask[r][threadIdx.x] = mask;
+                    if (mask) {
+                        const int ny = mp.cy + (r % 3) - 1;
+                        const int nz = mp.cz + (r / 3) - 1;
+                        const int m = mp.cx + P.gx * (ny + P.gy * nz);
+                        row_start[r][threadIdx.x] = mp.cx > 0
+                            ? slab_begin(f, m - 1, f.cell_start[m - 1], f.cell_start[m], mp.lmx)
+                            : f.cell_start[m];
+                    }
+                }
+                int r = 0;
+                uint32_t mask = row_mask[0][threadIdx.x];
+                int base = row_start[0][threadIdx.x];
+                for (int k = 0; k < found; ++k) {
+                    while (!mask) {
+                        ++r;
+                        mask = row_mask[r][threadIdx.x];
+                        base = row_start[r][threadIdx.x];
+                    }
+                    const int j = base + __ffs(mask) - 1;
+                    mask &= mask - 1u;
+                    force_pair(p, pev, f.pos[j], f.ev[j], P, a);
+                }
+            } else {
+                // Candidate scan (no masks, or a row longer than 32).
+                for (int r = 0; r < 9; ++r) {
+                    const int ny = mp.cy + (r % 3) - 1;
+                    const int nz = mp.cz + (r / 3) - 1;
+                    if (ny < 0 || ny >= P.gy || nz < 0 || nz >= P.gz) continue;
+                    const int m = mp.cx + P.gx * (ny + P.gy * nz);
+                    int begin, end;
+                    row_range(f, P, m, mp.cx, mp.lmx, mp.lmx, begin, end);
+                    for (int j = begin; j < end; ++j) {
+                        const float4 q = f.pos[j];
+                        const float rx = p.x - q.x, ry = p.y - q.y, rz = p.z - q.z;
+                        const float d2 = rx * rx + ry * ry + rz * rz;
+                        if (P.h2 < d2 || kFloatSmall > d2) continue;
+                        force_pair(p, pev, q, f.ev[j], P, a);
+                    }
                 }
             }
             write_force(f, P, self, p.w, a, false);
@@ -472,10 +530,10 @@ void launch_density(const Frame &f, const DevParams &P, int num_sms,
     k_density<<<num_sms * 8, kWarpsPerBlock * 32, 0, s>>>(f, P);
 }
 
-void launch_force(const Frame &f, const DevParams &P, int num_sms,
+void launch_force(const Frame &f, const DevParams &P, int num_sms, bool fresh,
                   cudaStream_t s) {
     if (f.n <= 0) return;
-    k_force<<<num_sms * 8, kWarpsPerBlock * 32, 0, s>>>(f, P);
+    k_force<<<num_sms * 8, kWarpsPerBlock * 32, 0, s>>>(f, P, fresh);
 }
 
 void launch_integrate(const Frame &f, const DevParams &P, cudaStream_t s) {

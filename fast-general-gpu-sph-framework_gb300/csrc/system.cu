@@ -70,6 +70,7 @@ struct System {
     Frame fr{};    // pointers shared by both parities
     double *red = nullptr;   // reductions workspace
     bool arranged = false;   // sorted state + split valid
+    bool lists_valid = false;   // TRA neighbour masks match the state
     uint64_t frames = 0;
 
     bool graph_mode = false;
@@ -153,6 +154,8 @@ struct System {
             (st = alloc_n(&fr.cell_prefix, size_t(max_occ))) ||
             (st = alloc_n(&fr.tasks, size_t(task_capacity))) ||
             (st = alloc_n(&fr.compact, N)) ||
+            (st = alloc_n(&fr.nbr_mask, ((N + 31) / 32) * 32 * 9)) ||
+            (st = alloc_n(&fr.nbr_flag, N)) ||
             (st = alloc_n(&fr.scan_tiles,
                           size_t((numc + kScanTile - 1) / kScanTile))) ||
             (st = alloc_n(&fr.scan_tiles4,
@@ -209,6 +212,7 @@ struct System {
     }
 
     void enqueue_arrange(int in) {
+        lists_valid = false;
         const Frame f = frame_arrange(in);
         launch_hash_count(f, dp, stream);
         launch_cell_scan(f, dp, stream);
@@ -216,9 +220,17 @@ struct System {
         launch_cell_sort(f, num_sms, stream);
         launch_split(f, dp, max_occ, stream);
     }
-    void enqueue_density(int b) { launch_density(frame_physics(b), dp, num_sms, stream); }
-    void enqueue_force(int b) { launch_force(frame_physics(b), dp, num_sms, stream); }
-    void enqueue_advance(int b) { launch_integrate(frame_physics(b), dp, stream); }
+    void enqueue_density(int b) {
+        launch_density(frame_physics(b), dp, num_sms, stream);
+        lists_valid = true;
+    }
+    void enqueue_force(int b) {
+        launch_force(frame_physics(b), dp, num_sms, lists_valid, stream);
+    }
+    void enqueue_advance(int b) {
+        launch_integrate(frame_physics(b), dp, stream);
+        lists_valid = false;
+    }
 
     gsph_status check_launch() {
         cudaError_t e = cudaGetLastError();
@@ -702,6 +714,7 @@ gsph_status gsph_copy_in(gsph_handle h, gsph_field field, const void *host_src,
     }
     GSPH_CUDA(cudaStreamSynchronize(s.stream));
     if (bytes) GSPH_CUDA(cudaMemcpy(dst, host_src, bytes, cudaMemcpyHostToDevice));
+    s.lists_valid = false;   // the masks describe the old state
     return GSPH_OK;
 }
 
@@ -718,6 +731,7 @@ gsph_status gsph_copy_in_async(gsph_handle h, gsph_field field,
     if (bytes)
         GSPH_CUDA(cudaMemcpyAsync(dst, host_src, bytes, cudaMemcpyHostToDevice,
                                   s.stream));
+    s.lists_valid = false;   // the masks describe the old state
     return GSPH_OK;
 }
 
