@@ -177,6 +177,8 @@ k_cell_scan_tiles(unsigned long long *__restrict__ tiles, int ntiles,
         ctr->num_big = 0;
         ctr->work_density = 0;
         ctr->work_force = 0;
+        ctr->work_density_sms = 0;
+        ctr->work_force_sms = 0;
     }
 }
 

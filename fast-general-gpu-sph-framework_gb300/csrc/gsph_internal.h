@@ -64,11 +64,13 @@ struct Counters {
     int32_t task_count;     // SMS tasks (T)
     int32_t middle;         // TRA particles
     int32_t n_sms;          // SMS particles
-    int32_t work_density;   // dynamic work counter of the density kernel
-    int32_t work_force;     // dynamic work counter of the force kernel
+    int32_t work_density;   // work counters of the persistent kernels:
+    int32_t work_force;     //   TRA units of density / force,
     uint32_t err;           // error bits
     int32_t err_index;      // first offending particle (best effort)
-    int32_t pad[23];
+    int32_t work_density_sms;   //   SMS tasks of density / force
+    int32_t work_force_sms;
+    int32_t pad[21];
 };
 
 // Per-frame device pointers of one scene.

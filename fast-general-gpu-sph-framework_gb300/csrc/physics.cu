@@ -88,14 +88,6 @@ __device__ __forceinline__ MicroPos micro_of(float4 p, const DevParams &P) {
     return r;
 }
 
-__device__ __forceinline__ float density_pair(float4 self, float4 q, float h2) {
-    const float dx = self.x - q.x, dy = self.y - q.y, dz = self.z - q.z;
-    const float d2 = dx * dx + dy * dy + dz * dz;
-    if (h2 < d2 || kFloatSmall > d2) return 0.f;
-    const float t = h2 - d2;
-    return t * t * t;
-}
-
 struct ForceAcc {
     float px, py, pz;   // pressure sum
     float vx, vy, vz;   // viscosity sum
@@ -180,205 +172,354 @@ __device__ __forceinline__ void write_force(const Frame &f, const DevParams &P,
     f.acc[self] = make_float4(tx + sx, ty + sy, tz + sz, 0.f);
 }
 
-constexpr int kWarpsPerBlock = 8;
+// Squared distances to staged candidates 2k and 2k+1 (x/y/z arrays), as a
+// pair; npx/npy/npz hold the negated self position twice. Same rounding as
+// dx*dx + dy*dy + dz*dz evaluated element by element.
+__device__ __forceinline__ float2 pair_d2(const float *sx, const float *sy,
+                                          const float *sz, int k, float2 npx,
+                                          float2 npy, float2 npz) {
+    const float2 dx = __fadd2_rn(reinterpret_cast<const float2 *>(sx)[k], npx);
+    const float2 dy = __fadd2_rn(reinterpret_cast<const float2 *>(sy)[k], npy);
+    const float2 dz = __fadd2_rn(reinterpret_cast<const float2 *>(sz)[k], npz);
+    float2 d2 = __fmul2_rn(dx, dx);
+    d2 = __ffma2_rn(dy, dy, d2);
+    return __ffma2_rn(dz, dz, d2);
+}
 
-// ---------------------------------------------------------------- density --
+constexpr int kWarpsPerBlock = 8;
+// SMS candidates staged per batch (two per lane).
+constexpr int kSmsBatch = 64;
+// Coordinate of padding candidates: far outside any kernel radius.
+constexpr float kFar = 1.0e18f;
+
+// Next work unit of a warp from a device counter (one atomic per unit).
+__device__ __forceinline__ int next_unit(int *counter) {
+    int u = 0;
+    if ((threadIdx.x & 31) == 0) u = atomicAdd(counter, 1);
+    return __shfl_sync(kFull, u, 0);
+}
+
+// ------------------------------------------------------------ density TRA --
+// One particle per lane, 32 consecutive TRA particles per work unit
+// (density_kernels.cu:318-366). Which candidates of each row interact is also
+// recorded as a bit mask for the force pass.
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, 6)
-k_density(Frame f, DevParams P) {
-    __shared__ float4 stage[kWarpsPerBlock][32];
+k_density_tra(Frame f, DevParams P) {
     const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
     const int middle = f.ctr->middle;
-    const int task_count = f.ctr->task_count;
-    const int tra_units = (middle + 31) >> 5;
-    const int total = tra_units + task_count;
+    const int units = (middle + 31) >> 5;
     for (;;) {
-        int u = 0;
-        if (lane == 0) u = atomicAdd(&f.ctr->work_density, 1);
-        u = __shfl_sync(kFull, u, 0);
-        if (u >= total) break;
-        if (u < tra_units) {
-            // TRA: one particle per lane (density_kernels.cu:318-366). Which
-            // candidates of each row interact is also recorded as a bit mask
-            // for the force pass.
-            const int idx = (u << 5) + lane;
-            if (idx >= middle) continue;
-            const int self = f.compact[idx];
-            const float4 p = f.pos[self];
-            const MicroPos mp = micro_of(p, P);
-            uint32_t *masks = f.nbr_mask + size_t(u) * 9 * 32 + lane;
-            int incomplete = 0;
-            int found = 0;
-            float sum = 0.f;
-            for (int r = 0; r < 9; ++r) {
-                const int ny = mp.cy + (r % 3) - 1;
-                const int nz = mp.cz + (r / 3) - 1;
-                uint32_t mask = 0u;
-                if (ny >= 0 && ny < P.gy && nz >= 0 && nz < P.gz) {
-                    const int m = mp.cx + P.gx * (ny + P.gy * nz);
-                    int begin, end;
-                    row_range(f, P, m, mp.cx, mp.lmx, mp.lmx, begin, end);
-                    incomplete |= (end - begin > kMaskRowMax);
-                    uint32_t bit = 1u;
-#pragma unroll 4
-                    for (int j = begin; j < end; ++j, bit <<= 1) {
-                        const float4 q = f.pos[j];
-                        const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
-                        const float d2 = dx * dx + dy * dy + dz * dz;
-                        if (P.h2 < d2 || kFloatSmall > d2) continue;
-                        const float t = P.h2 - d2;
-                        sum += t * t * t;
-                        mask |= bit;
-                    }
-                }
-                masks[r * 32] = mask;
-                found += __popc(mask);
-            }
-            f.nbr_flag[idx] = incomplete ? -1 : found;
-            write_density(f, P, self, sum, false);
-        } else {
-            // SMS: one 32-particle task per warp (density_kernels.cu:368-565).
-            const gsph_block_task task = f.tasks[u - tra_units];
-            const int cb = task.cell_begin;
-            const int cend = cb + task.cell_particle_count;
-            const int self = cb + task.p_offset + lane;
-            const bool active = self < cend;
-            if (cb + int(task.p_offset) >= cend) continue;   // warp-uniform
-            const float4 p = f.pos[active ? self : cend - 1];
-            const int cx = task.cell_pos[0], cy = task.cell_pos[1],
-                      cz = task.cell_pos[2];
-            float sum = 0.f;
-            for (int r = 0; r < 9; ++r) {
-                const int ny = cy + (r % 3) - 1;
-                const int nz = cz + (r / 3) - 1;
-                if (ny < 0 || ny >= P.gy || nz < 0 || nz >= P.gz) continue;
-                const int m = cx + P.gx * (ny + P.gy * nz);
+        const int u = next_unit(&f.ctr->work_density);
+        if (u >= units) break;
+        const int idx = (u << 5) + lane;
+        if (idx >= middle) continue;
+        const int self = f.compact[idx];
+        const float4 p = f.pos[self];
+        const MicroPos mp = micro_of(p, P);
+        uint32_t *masks = f.nbr_mask + size_t(u) * 9 * 32 + lane;
+        int incomplete = 0;
+        int found = 0;
+        float sum = 0.f;
+        for (int r = 0; r < 9; ++r) {
+            const int ny = mp.cy + (r % 3) - 1;
+            const int nz = mp.cz + (r / 3) - 1;
+            uint32_t mask = 0u;
+            if (ny >= 0 && ny < P.gy && nz >= 0 && nz < P.gz) {
+                const int m = mp.cx + P.gx * (ny + P.gy * nz);
                 int begin, end;
-                row_range(f, P, m, cx, task.xxi, task.xxx, begin, end);
-                for (int base = begin; base < end; base += 32) {
-                    const int cnt = min(32, end - base);
-                    if (lane < cnt) stage[warp][lane] = f.pos[base + lane];
-                    __syncwarp();
-                    for (int k = 0; k < cnt; ++k)
-                        sum += density_pair(p, stage[warp][k], P.h2);
-                    __syncwarp();
+                row_range(f, P, m, mp.cx, mp.lmx, mp.lmx, begin, end);
+                incomplete |= (end - begin > kMaskRowMax);
+                uint32_t bit = 1u;
+#pragma unroll 4
+                for (int j = begin; j < end; ++j, bit <<= 1) {
+                    const float4 q = f.pos[j];
+                    const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+                    const float d2 = dx * dx + dy * dy + dz * dz;
+                    if (P.h2 < d2 || kFloatSmall > d2) continue;
+                    const float t = P.h2 - d2;
+                    sum += t * t * t;
+                    mask |= bit;
                 }
             }
-            if (active) write_density(f, P, self, sum, true);
+            masks[r * 32] = mask;
+            found += __popc(mask);
         }
+        f.nbr_flag[idx] = incomplete ? -1 : found;
+        write_density(f, P, self, sum, false);
     }
 }
 
-// ------------------------------------------------------------------ force --
+// Stage candidates [base, base + cnt) of the sorted arrays into a warp's
+// shared arrays (two per lane); slots past cnt get far-away padding.
+__device__ __forceinline__ void stage_xyz(const Frame &f, int base, int cnt,
+                                          float *sx, float *sy, float *sz,
+                                          float4 *sp, float4 *sv, int lane) {
+#pragma unroll
+    for (int h = 0; h < kSmsBatch; h += 32) {
+        const int t = h + lane;
+        float4 q = make_float4(kFar, kFar, kFar, 0.f);
+        float4 qv = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (t < cnt) {
+            q = f.pos[base + t];
+            if (sv) qv = f.ev[base + t];
+        }
+        sx[t] = q.x;
+        sy[t] = q.y;
+        sz[t] = q.z;
+        if (sp) sp[t] = q;
+        if (sv) sv[t] = qv;
+    }
+}
+
+// ------------------------------------------------------------ density SMS --
+// One 32-particle task per warp (density_kernels.cu:368-565). Candidates are
+// staged 64 at a time as x/y/z arrays in shared memory; every lane evaluates
+// them two at a time with packed FP32x2 arithmetic (distances and h^2 - r^2
+// round exactly as the scalar form).
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 6)
+k_density_sms(Frame f, DevParams P) {
+    __shared__ __align__(16) float sms_x[kWarpsPerBlock][kSmsBatch];
+    __shared__ __align__(16) float sms_y[kWarpsPerBlock][kSmsBatch];
+    __shared__ __align__(16) float sms_z[kWarpsPerBlock][kSmsBatch];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int task_count = f.ctr->task_count;
+    float *sx = sms_x[warp], *sy = sms_y[warp], *sz = sms_z[warp];
+    for (;;) {
+        const int u = next_unit(&f.ctr->work_density_sms);
+        if (u >= task_count) break;
+        const gsph_block_task task = f.tasks[u];
+        const int cb = task.cell_begin;
+        const int cend = cb + task.cell_particle_count;
+        const int self = cb + task.p_offset + lane;
+        const bool active = self < cend;
+        if (cb + int(task.p_offset) >= cend) continue;   // warp-uniform
+        const float4 p = f.pos[active ? self : cend - 1];
+        const int cx = task.cell_pos[0], cy = task.cell_pos[1],
+                  cz = task.cell_pos[2];
+        const float2 npx = make_float2(-p.x, -p.x);
+        const float2 npy = make_float2(-p.y, -p.y);
+        const float2 npz = make_float2(-p.z, -p.z);
+        const float2 h2v = make_float2(P.h2, P.h2);
+        const float2 m1 = make_float2(-1.f, -1.f);
+        float2 acc = make_float2(0.f, 0.f);
+        for (int r = 0; r < 9; ++r) {
+            const int ny = cy + (r % 3) - 1;
+            const int nz = cz + (r / 3) - 1;
+            if (ny < 0 || ny >= P.gy || nz < 0 || nz >= P.gz) continue;
+            const int m = cx + P.gx * (ny + P.gy * nz);
+            int begin, end;
+            row_range(f, P, m, cx, task.xxi, task.xxx, begin, end);
+            for (int base = begin; base < end; base += kSmsBatch) {
+                const int cnt = min(kSmsBatch, end - base);
+                stage_xyz(f, base, cnt, sx, sy, sz, nullptr, nullptr, lane);
+                __syncwarp();
+                const int pairs = (cnt + 1) >> 1;
+#pragma unroll 4
+                for (int k = 0; k < pairs; ++k) {
+                    const float2 d2 = pair_d2(sx, sy, sz, k, npx, npy, npz);
+                    float2 t = __ffma2_rn(d2, m1, h2v);
+                    t.x = (t.x < 0.f || d2.x < kFloatSmall) ? 0.f : t.x;
+                    t.y = (t.y < 0.f || d2.y < kFloatSmall) ? 0.f : t.y;
+                    acc = __ffma2_rn(__fmul2_rn(t, t), t, acc);
+                }
+                __syncwarp();
+            }
+        }
+        if (active) write_density(f, P, self, acc.x + acc.y, true);
+    }
+}
+
+// -------------------------------------------------------------- force TRA --
+// The neighbours the density pass found, in the same order (rows in sequence,
+// set bits in increasing candidate index). Each lane stages its 9 (row start,
+// mask) pairs in shared memory and walks all its neighbours in one loop, so
+// lanes stay converged across rows. Without masks (or with a row longer than
+// 32 candidates) the lane scans its candidates as the reference does.
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
-k_force(Frame f, DevParams P, bool fresh) {
-    __shared__ float4 stage_p[kWarpsPerBlock][32];
-    __shared__ float4 stage_v[kWarpsPerBlock][32];
+k_force_tra(Frame f, DevParams P, bool fresh) {
     __shared__ uint32_t row_mask[9][kWarpsPerBlock * 32];
     __shared__ int row_start[9][kWarpsPerBlock * 32];
     const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
     const int middle = f.ctr->middle;
-    const int task_count = f.ctr->task_count;
-    const int tra_units = (middle + 31) >> 5;
-    const int total = tra_units + task_count;
+    const int units = (middle + 31) >> 5;
     for (;;) {
-        int u = 0;
-        if (lane == 0) u = atomicAdd(&f.ctr->work_force, 1);
-        u = __shfl_sync(kFull, u, 0);
-        if (u >= total) break;
+        const int u = next_unit(&f.ctr->work_force);
+        if (u >= units) break;
+        const int idx = (u << 5) + lane;
+        if (idx >= middle) continue;
+        const int self = f.compact[idx];
+        const float4 p = f.pos[self];
+        const float4 pev = f.ev[self];
+        const MicroPos mp = micro_of(p, P);
         ForceAcc a = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        if (u < tra_units) {
-            const int idx = (u << 5) + lane;
-            if (idx >= middle) continue;
-            const int self = f.compact[idx];
-            const float4 p = f.pos[self];
-            const float4 pev = f.ev[self];
-            const MicroPos mp = micro_of(p, P);
-            const int found = fresh ? f.nbr_flag[idx] : -1;
-            if (found >= 0) {
-                // The neighbours the density pass found, in the same order:
-                // rows in sequence, set bits in increasing candidate index.
-                // Each lane stages its 9 (row start, mask) pairs in shared
-                // memory and walks all its neighbours in one loop, so lanes
-                // stay converged across rows.
-                const uint32_t *masks = f.nbr_mask + size_t(u) * 9 * 32 + lane;
-                for (int r = 0; r < 9; ++r) {
-                    const uint32_t mask = masks[r * 32];
-                    row_mask[r][threadIdx.x] = mask;
-                    if (mask) {
-                        const int ny = mp.cy + (r % 3) - 1;
-                        const int nz = mp.cz + (r / 3) - 1;
-                        const int m = mp.cx + P.gx * (ny + P.gy * nz);
-                        row_start[r][threadIdx.x] = mp.cx > 0
-                            ? slab_begin(f, m - 1, f.cell_start[m - 1], f.cell_start[m], mp.lmx)
-                            : f.cell_start[m];
-                    }
-                }
-                int r = 0;
-                uint32_t mask = row_mask[0][threadIdx.x];
-                int base = row_start[0][threadIdx.x];
-                for (int k = 0; k < found; ++k) {
-                    while (!mask) {
-                        ++r;
-                        mask = row_mask[r][threadIdx.x];
-                        base = row_start[r][threadIdx.x];
-                    }
-                    const int j = base + __ffs(mask) - 1;
-                    mask &= mask - 1u;
-                    force_pair(p, pev, f.pos[j], f.ev[j], P, a);
-                }
-            } else {
-                // Candidate scan (no masks, or a row longer than 32).
-                for (int r = 0; r < 9; ++r) {
+        const int found = fresh ? f.nbr_flag[idx] : -1;
+        if (found >= 0) {
+            const uint32_t *masks = f.nbr_mask + size_t(u) * 9 * 32 + lane;
+            for (int r = 0; r < 9; ++r) {
+                const uint32_t mask = masks[r * 32];
+                row_mask[r][threadIdx.x] = mask;
+                if (mask) {
                     const int ny = mp.cy + (r % 3) - 1;
                     const int nz = mp.cz + (r / 3) - 1;
-                    if (ny < 0 || ny >= P.gy || nz < 0 || nz >= P.gz) continue;
                     const int m = mp.cx + P.gx * (ny + P.gy * nz);
-                    int begin, end;
-                    row_range(f, P, m, mp.cx, mp.lmx, mp.lmx, begin, end);
-                    for (int j = begin; j < end; ++j) {
-                        const float4 q = f.pos[j];
-                        const float rx = p.x - q.x, ry = p.y - q.y, rz = p.z - q.z;
-                        const float d2 = rx * rx + ry * ry + rz * rz;
-                        if (P.h2 < d2 || kFloatSmall > d2) continue;
-                        force_pair(p, pev, q, f.ev[j], P, a);
-                    }
+                    row_start[r][threadIdx.x] = mp.cx > 0
+                        ? slab_begin(f, m - 1, f.cell_start[m - 1], f.cell_start[m], mp.lmx)
+                        : f.cell_start[m];
                 }
             }
-            write_force(f, P, self, p.w, a, false);
+            int r = 0;
+            uint32_t mask = row_mask[0][threadIdx.x];
+            int base = row_start[0][threadIdx.x];
+            for (int k = 0; k < found; ++k) {
+                while (!mask) {
+                    ++r;
+                    mask = row_mask[r][threadIdx.x];
+                    base = row_start[r][threadIdx.x];
+                }
+                const int j = base + __ffs(mask) - 1;
+                mask &= mask - 1u;
+                force_pair(p, pev, f.pos[j], f.ev[j], P, a);
+            }
         } else {
-            const gsph_block_task task = f.tasks[u - tra_units];
-            const int cb = task.cell_begin;
-            const int cend = cb + task.cell_particle_count;
-            const int self = cb + task.p_offset + lane;
-            const bool active = self < cend;
-            if (cb + int(task.p_offset) >= cend) continue;
-            const int safe = active ? self : cend - 1;
-            const float4 p = f.pos[safe];
-            const float4 pev = f.ev[safe];
-            const int cx = task.cell_pos[0], cy = task.cell_pos[1],
-                      cz = task.cell_pos[2];
             for (int r = 0; r < 9; ++r) {
-                const int ny = cy + (r % 3) - 1;
-                const int nz = cz + (r / 3) - 1;
+                const int ny = mp.cy + (r % 3) - 1;
+                const int nz = mp.cz + (r / 3) - 1;
                 if (ny < 0 || ny >= P.gy || nz < 0 || nz >= P.gz) continue;
-                const int m = cx + P.gx * (ny + P.gy * nz);
+                const int m = mp.cx + P.gx * (ny + P.gy * nz);
                 int begin, end;
-                row_range(f, P, m, cx, task.xxi, task.xxx, begin, end);
-                for (int base = begin; base < end; base += 32) {
-                    const int cnt = min(32, end - base);
-                    if (lane < cnt) {
-                        stage_p[warp][lane] = f.pos[base + lane];
-                        stage_v[warp][lane] = f.ev[base + lane];
-                    }
-                    __syncwarp();
-                    for (int k = 0; k < cnt; ++k)
-                        force_pair(p, pev, stage_p[warp][k], stage_v[warp][k], P, a);
-                    __syncwarp();
+                row_range(f, P, m, mp.cx, mp.lmx, mp.lmx, begin, end);
+                for (int j = begin; j < end; ++j) {
+                    const float4 q = f.pos[j];
+                    const float rx = p.x - q.x, ry = p.y - q.y, rz = p.z - q.z;
+                    const float d2 = rx * rx + ry * ry + rz * rz;
+                    if (P.h2 < d2 || kFloatSmall > d2) continue;
+                    force_pair(p, pev, q, f.ev[j], P, a);
                 }
             }
-            if (active) write_force(f, P, self, p.w, a, true);
+        }
+        write_force(f, P, self, p.w, a, false);
+    }
+}
+
+// -------------------------------------------------------------- force SMS --
+// One 32-particle task per warp (force_kernels.cu:830-1054). Candidates are
+// staged 64 at a time as structure-of-arrays in shared memory and evaluated
+// two at a time with packed FP32x2 arithmetic; a pair is skipped when no lane
+// of the warp interacts with either candidate. Each term rounds as the
+// reference's scalar expression; the two halves of every accumulator are
+// summed at the end.
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 4)
+k_force_sms(Frame f, DevParams P) {
+    __shared__ __align__(16) float sm[8][kWarpsPerBlock][kSmsBatch];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int task_count = f.ctr->task_count;
+    float *sx = sm[0][warp], *sy = sm[1][warp], *sz = sm[2][warp], *sw = sm[3][warp];
+    float *svx = sm[4][warp], *svy = sm[5][warp], *svz = sm[6][warp], *spr = sm[7][warp];
+    for (;;) {
+        const int u = next_unit(&f.ctr->work_force_sms);
+        if (u >= task_count) break;
+        const gsph_block_task task = f.tasks[u];
+        const int cb = task.cell_begin;
+        const int cend = cb + task.cell_particle_count;
+        const int self = cb + task.p_offset + lane;
+        const bool active = self < cend;
+        if (cb + int(task.p_offset) >= cend) continue;
+        const int safe = active ? self : cend - 1;
+        const float4 p = f.pos[safe];
+        const float4 pev = f.ev[safe];
+        const int cx = task.cell_pos[0], cy = task.cell_pos[1],
+                  cz = task.cell_pos[2];
+        const float2 npx = make_float2(-p.x, -p.x);
+        const float2 npy = make_float2(-p.y, -p.y);
+        const float2 npz = make_float2(-p.z, -p.z);
+        const float2 nvx = make_float2(-pev.x, -pev.x);
+        const float2 nvy = make_float2(-pev.y, -pev.y);
+        const float2 nvz = make_float2(-pev.z, -pev.z);
+        const float2 pi2 = make_float2(pev.w, pev.w);
+        const float2 h2v = make_float2(P.h2, P.h2);
+        const float2 hv = make_float2(P.h, P.h);
+        const float2 m1 = make_float2(-1.f, -1.f);
+        const float2 m075 = make_float2(-0.75f, -0.75f);
+        const float2 zero = make_float2(0.f, 0.f);
+        // pressure sum gets -r*ps = d*ps with d = q - p; the colour
+        // gradient is accumulated with the opposite sign and negated at the end
+        float2 Px = zero, Py = zero, Pz = zero, Vx = zero, Vy = zero, Vz = zero;
+        float2 Gx = zero, Gy = zero, Gz = zero, L = zero;
+        for (int r = 0; r < 9; ++r) {
+            const int ny = cy + (r % 3) - 1;
+            const int nz = cz + (r / 3) - 1;
+            if (ny < 0 || ny >= P.gy || nz < 0 || nz >= P.gz) continue;
+            const int m = cx + P.gx * (ny + P.gy * nz);
+            int begin, end;
+            row_range(f, P, m, cx, task.xxi, task.xxx, begin, end);
+            for (int base = begin; base < end; base += kSmsBatch) {
+                const int cnt = min(kSmsBatch, end - base);
+#pragma unroll
+                for (int hh = 0; hh < kSmsBatch; hh += 32) {
+                    const int t = hh + lane;
+                    float4 q = make_float4(kFar, kFar, kFar, 0.f);
+                    float4 qv = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (t < cnt) {
+                        q = f.pos[base + t];
+                        qv = f.ev[base + t];
+                    }
+                    sx[t] = q.x; sy[t] = q.y; sz[t] = q.z; sw[t] = q.w;
+                    svx[t] = qv.x; svy[t] = qv.y; svz[t] = qv.z; spr[t] = qv.w;
+                }
+                __syncwarp();
+                const int pairs = (cnt + 1) >> 1;
+                for (int k = 0; k < pairs; ++k) {
+                    const float2 dx = __fadd2_rn(reinterpret_cast<const float2 *>(sx)[k], npx);
+                    const float2 dy = __fadd2_rn(reinterpret_cast<const float2 *>(sy)[k], npy);
+                    const float2 dz = __fadd2_rn(reinterpret_cast<const float2 *>(sz)[k], npz);
+                    float2 d2 = __fmul2_rn(dx, dx);
+                    d2 = __ffma2_rn(dy, dy, d2);
+                    d2 = __ffma2_rn(dz, dz, d2);
+                    const float2 t = __ffma2_rn(d2, m1, h2v);   // h^2 - r^2
+                    const bool okx = t.x >= 0.f && d2.x >= kFloatSmall;
+                    const bool oky = t.y >= 0.f && d2.y >= kFloatSmall;
+                    if (!__any_sync(kFull, active && (okx || oky))) continue;
+                    const float2 d2s = make_float2(okx ? d2.x : 1.f, oky ? d2.y : 1.f);
+                    const float2 inv = make_float2(rsqrtf(d2s.x), rsqrtf(d2s.y));
+                    const float2 d = __fmul2_rn(d2s, inv);
+                    const float2 kk = __ffma2_rn(d, m1, hv);       // h - r
+                    const float2 V = reinterpret_cast<const float2 *>(sw)[k];
+                    float2 wk = __fmul2_rn(V, kk);
+                    wk = make_float2(okx ? wk.x : 0.f, oky ? wk.y : 0.f);
+                    const float2 psum = __fadd2_rn(pi2, reinterpret_cast<const float2 *>(spr)[k]);
+                    const float2 ps = __fmul2_rn(__fmul2_rn(__fmul2_rn(wk, psum), kk), inv);
+                    Px = __ffma2_rn(dx, ps, Px);
+                    Py = __ffma2_rn(dy, ps, Py);
+                    Pz = __ffma2_rn(dz, ps, Pz);
+                    Vx = __ffma2_rn(__fadd2_rn(reinterpret_cast<const float2 *>(svx)[k], nvx), wk, Vx);
+                    Vy = __ffma2_rn(__fadd2_rn(reinterpret_cast<const float2 *>(svy)[k], nvy), wk, Vy);
+                    Vz = __ffma2_rn(__fadd2_rn(reinterpret_cast<const float2 *>(svz)[k], nvz), wk, Vz);
+                    float2 wh = __fmul2_rn(V, t);
+                    wh = make_float2(okx ? wh.x : 0.f, oky ? wh.y : 0.f);
+                    const float2 gw = __fmul2_rn(wh, t);
+                    Gx = __ffma2_rn(dx, gw, Gx);
+                    Gy = __ffma2_rn(dy, gw, Gy);
+                    Gz = __ffma2_rn(dz, gw, Gz);
+                    L = __ffma2_rn(wh, __ffma2_rn(t, m075, d2), L);
+                }
+                __syncwarp();
+            }
+        }
+        if (active) {
+            ForceAcc a;
+            a.px = Px.x + Px.y;
+            a.py = Py.x + Py.y;
+            a.pz = Pz.x + Pz.y;
+            a.vx = Vx.x + Vx.y;
+            a.vy = Vy.x + Vy.y;
+            a.vz = Vz.x + Vz.y;
+            a.gx = -(Gx.x + Gx.y);
+            a.gy = -(Gy.x + Gy.y);
+            a.gz = -(Gz.x + Gz.y);
+            a.lap = L.x + L.y;
+            write_force(f, P, self, p.w, a, true);
         }
     }
 }
@@ -527,13 +668,15 @@ k_final_sum(const double *__restrict__ part, int nparts, double *__restrict__ ou
 void launch_density(const Frame &f, const DevParams &P, int num_sms,
                     cudaStream_t s) {
     if (f.n <= 0) return;
-    k_density<<<num_sms * 8, kWarpsPerBlock * 32, 0, s>>>(f, P);
+    k_density_tra<<<num_sms * 6, kWarpsPerBlock * 32, 0, s>>>(f, P);
+    k_density_sms<<<num_sms * 6, kWarpsPerBlock * 32, 0, s>>>(f, P);
 }
 
 void launch_force(const Frame &f, const DevParams &P, int num_sms, bool fresh,
                   cudaStream_t s) {
     if (f.n <= 0) return;
-    k_force<<<num_sms * 8, kWarpsPerBlock * 32, 0, s>>>(f, P, fresh);
+    k_force_tra<<<num_sms * 5, kWarpsPerBlock * 32, 0, s>>>(f, P, fresh);
+    k_force_sms<<<num_sms * 4, kWarpsPerBlock * 32, 0, s>>>(f, P);
 }
 
 void launch_integrate(const Frame &f, const DevParams &P, cudaStream_t s) {
