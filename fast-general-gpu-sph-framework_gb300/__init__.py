@@ -133,6 +133,7 @@ class Info(C.Structure):
         ("tra_particles", C.c_int32), ("sms_tasks", C.c_int32),
         ("occupied_cells", C.c_int32), ("big_cells", C.c_int32),
         ("frames", C.c_uint64), ("device_bytes", C.c_uint64),
+        ("n_scenes", C.c_uint32), ("reserved_", C.c_uint32),
     ]
 
 
@@ -167,6 +168,10 @@ _SIGS = {
     "gsph_create": ([C.POINTER(Params), _VP, _VP, C.c_uint32, C.c_int, C.POINTER(_VP)], C.c_int),
     "gsph_create_from_json": ([C.c_char_p, C.c_int, C.POINTER(_VP)], C.c_int),
     "gsph_destroy": ([_VP], C.c_int),
+    "gsph_batch_create": ([C.POINTER(Params), C.POINTER(C.c_uint32), C.c_uint32, _VP, _VP,
+                           C.c_int, C.POINTER(_VP)], C.c_int),
+    "gsph_batch_ranges": ([_VP, _VP, _VP], C.c_int),
+    "gsph_copy_out_scene": ([_VP, C.c_uint32, C.c_int, _VP, C.c_size_t], C.c_int),
     "gsph_step": ([_VP, C.c_int], C.c_int),
     "gsph_arrange": ([_VP], C.c_int),
     "gsph_density": ([_VP], C.c_int),
@@ -426,3 +431,61 @@ class HybridSystem:
     @property
     def handle(self) -> int:
         return self._h.value
+
+
+class Batch(HybridSystem):
+    """Several independent scenes stepped together (gsph_batch_create): one
+    launch per stage for all of them. Scene k evolves exactly as it would
+    alone (bit-identical). `scenes` is a list of (params, positions[,
+    velocities]) with a common physical parameter set."""
+
+    def __init__(self, scenes, device: int = 0):
+        lib = load_library()
+        S = len(scenes)
+        plist = (Params * S)()
+        counts = (C.c_uint32 * S)()
+        pos_parts, vel_parts = [], []
+        for k, sc in enumerate(scenes):
+            p, pos = sc[0], np.ascontiguousarray(sc[1], np.float32).reshape(-1, 4)
+            vel = (np.ascontiguousarray(sc[2], np.float32).reshape(-1, 4)
+                   if len(sc) > 2 and sc[2] is not None else np.zeros_like(pos))
+            C.memmove(C.addressof(plist[k]), C.addressof(p), C.sizeof(Params))
+            counts[k] = len(pos)
+            pos_parts.append(pos)
+            vel_parts.append(vel)
+        pos_all = np.concatenate(pos_parts) if pos_parts else np.zeros((0, 4), np.float32)
+        vel_all = np.concatenate(vel_parts) if vel_parts else np.zeros((0, 4), np.float32)
+        h = C.c_void_p()
+        _check(lib.gsph_batch_create(plist, counts, S,
+                                     _ptr(pos_all) if len(pos_all) else None,
+                                     _ptr(vel_all) if len(vel_all) else None,
+                                     device, C.byref(h)))
+        self._h = h
+        self._lib = lib
+        self.params = Params()
+        _check(lib.gsph_get_params(h, C.byref(self.params)))
+        self.n = int(self.info().n_particles)
+        self.num_scenes = S
+        self.pbase = np.empty(S + 1, np.int32)
+        self.cbase = np.empty(S + 1, np.int32)
+        _check(lib.gsph_batch_ranges(h, _ptr(self.pbase), _ptr(self.cbase)))
+
+    def copy_out_scene(self, scene: int, field: int) -> np.ndarray:
+        n = int(self.pbase[scene + 1] - self.pbase[scene])
+        nc = int(self.cbase[scene + 1] - self.cbase[scene])
+        if field in (FIELD_POSITION, FIELD_VELOCITY, FIELD_EVAL_VELOCITY, FIELD_ACCELERATION):
+            out = np.empty((n, 4), np.float32)
+        elif field == FIELD_KEY:
+            out = np.empty(n, np.uint32)
+        elif field == FIELD_PERMUTATION:
+            out = np.empty(n, np.int32)
+        elif field == FIELD_CELL_START:
+            out = np.empty(nc + 1, np.int32)
+        elif field == FIELD_CELL_COUNT:
+            out = np.empty(nc, np.int32)
+        else:
+            raise ValueError(f"field {field} has no per-scene form")
+        _check(self._lib.gsph_copy_out_scene(self._h, scene, field,
+                                             _ptr(out) if out.size else _ptr(np.empty(1, np.uint8)),
+                                             out.nbytes))
+        return out

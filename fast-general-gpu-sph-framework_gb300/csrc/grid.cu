@@ -36,29 +36,31 @@ __device__ __forceinline__ unsigned lanemask_lt() {
     return m;
 }
 
-// Micro key of one position (sph_utils.cuh:44-99). Positions outside the grid
-// raise kErrOutOfDomain and are clamped to the nearest cell so that no index
-// ever leaves the tables.
+// Micro key of one position (sph_utils.cuh:44-99), in the global cell space
+// of a batch: the scene's cell base is added to the reference's cell index.
+// Positions outside the scene's grid raise kErrOutOfDomain and are clamped to
+// the nearest cell so that no index ever leaves the tables.
 __device__ __forceinline__ uint32_t micro_key(float4 p, const DevParams &P,
+                                              const SceneGeom &G,
                                               Counters *ctr, int i) {
     const float fx = floorf(p.x * P.rat);
     const float fy = floorf(p.y * P.rat);
     const float fz = floorf(p.z * P.rat);
-    const float lx = float(P.gx << 2), ly = float(P.gy << 2),
-                lz = float(P.gz << 2);
+    const float lx = float(G.gx << 2), ly = float(G.gy << 2),
+                lz = float(G.gz << 2);
     int mx, my, mz;
     if (fx >= 0.f && fx < lx && fy >= 0.f && fy < ly && fz >= 0.f && fz < lz) {
         mx = int(fx);
         my = int(fy);
         mz = int(fz);
     } else {
-        mx = (fx >= 0.f) ? min(int(fminf(fx, lx - 1.f)), (P.gx << 2) - 1) : 0;
-        my = (fy >= 0.f) ? min(int(fminf(fy, ly - 1.f)), (P.gy << 2) - 1) : 0;
-        mz = (fz >= 0.f) ? min(int(fminf(fz, lz - 1.f)), (P.gz << 2) - 1) : 0;
+        mx = (fx >= 0.f) ? min(int(fminf(fx, lx - 1.f)), (G.gx << 2) - 1) : 0;
+        my = (fy >= 0.f) ? min(int(fminf(fy, ly - 1.f)), (G.gy << 2) - 1) : 0;
+        mz = (fz >= 0.f) ? min(int(fminf(fz, lz - 1.f)), (G.gz << 2) - 1) : 0;
         if (atomicOr(&ctr->err, kErrOutOfDomain) == 0u) ctr->err_index = i;
     }
-    const uint32_t c = uint32_t(mx >> 2) +
-                       uint32_t(P.gx) * (uint32_t(my >> 2) + uint32_t(P.gy) * uint32_t(mz >> 2));
+    const uint32_t c = uint32_t(G.cbase) + uint32_t(mx >> 2) +
+                       uint32_t(G.gx) * (uint32_t(my >> 2) + uint32_t(G.gy) * uint32_t(mz >> 2));
     const uint32_t sub = uint32_t(my & 3) | (uint32_t(mz & 3) << 2) | (uint32_t(mx & 3) << 4);
     return (c << 6) | sub;
 }
@@ -66,14 +68,15 @@ __device__ __forceinline__ uint32_t micro_key(float4 p, const DevParams &P,
 // ---------------------------------------------------------------------------
 // A2: key + per-coarse-cell slot (warp-aggregated atomics).
 __global__ void __launch_bounds__(256)
-k_hash_count(const float4 *__restrict__ pos, int n, DevParams P,
+k_hash_count(const float4 *__restrict__ pos, int n, DevParams P, SceneTable T,
              uint32_t *__restrict__ key_out, uint32_t *__restrict__ slot_out,
              int32_t *__restrict__ cell_count, Counters *ctr) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < n;
     const unsigned active = __ballot_sync(kFull, valid);
     if (!valid) return;
-    const uint32_t key = micro_key(pos[i], P, ctr, i);
+    const SceneGeom G = geom_of_particle(T, i);
+    const uint32_t key = micro_key(pos[i], P, G, ctr, i);
     const uint32_t cell = key >> 6;
     const unsigned peers = __match_any_sync(active, cell);
     const int lane = threadIdx.x & 31;
@@ -321,8 +324,9 @@ __global__ void __launch_bounds__(256) k_sort_big(Frame f) {
 
 void launch_hash_count(const Frame &f, const DevParams &P, cudaStream_t s) {
     if (f.n <= 0) return;
-    k_hash_count<<<(f.n + 255) / 256, 256, 0, s>>>(f.pos_in, f.n, P, f.key_in,
-                                                  f.slot, f.cell_count, f.ctr);
+    k_hash_count<<<(f.n + 255) / 256, 256, 0, s>>>(f.pos_in, f.n, P, f.scenes,
+                                                  f.key_in, f.slot, f.cell_count,
+                                                  f.ctr);
 }
 
 void launch_cell_scan(const Frame &f, const DevParams &P, cudaStream_t s) {

@@ -43,19 +43,65 @@ enum : uint32_t {
     kErrTaskCapacity = 2u,    // more SMS tasks than the task buffer holds
 };
 
-// Parameters as the kernels see them (passed by value: one constant bank per
-// launch, so several scenes/handles can coexist in one process).
+// Physical parameters as the kernels see them (passed by value: one constant
+// bank per launch, so several handles can coexist in one process). Every
+// scene of a batch shares them; per-scene geometry lives in SceneGeom.
 struct DevParams {
     float h, h2, rat;            // rat = 4 * inv_cell_size (micro cells)
-    int gx, gy, gz, numc;
+    int numc;                    // cells of all scenes
     float density_scale, self_density, rest_density, inv_rest_density;
     float gas_constant;
     float half_spiky, visco_coef, grad_color_scale, lplc_color_scale;
     float surface_normal, surface_coe, mass;
     float time_step, wall_damping, wall_kernel;   // wall_kernel = h + 0.01
     float gx_acc, gy_acc, gz_acc;                 // gravity
-    float bmin_x, bmin_y, bmin_z, bmax_x, bmax_y, bmax_z;
+    float bmin;                                   // lower wall (= h) on every axis
 };
+
+// Geometry of one scene of a batch. Particles of scene s occupy
+// [pbase, pbase + n) and its cells [cbase, cbase + gx*gy*gz) of the
+// concatenated arrays; positions are in the scene's own coordinates. A single
+// scene is a batch of one.
+struct SceneGeom {
+    int gx, gy, gz;
+    int cbase;
+    float bmax_x, bmax_y, bmax_z;
+    int pad;
+};
+
+// Scenes of a batch. With one scene (count == 1) the geometry travels in the
+// kernel parameter itself (`single`) and the device arrays are not read.
+struct SceneTable {
+    const SceneGeom *geom;   // [count]
+    const int *pbase;        // [count + 1] particle offsets
+    const int *cbase;        // [count + 1] cell offsets
+    int count;
+    SceneGeom single;
+};
+
+// Geometry of the scene holding sorted particle i / global cell c.
+__device__ __forceinline__ int scene_of(const int *base, int count, int i);
+__device__ __forceinline__ SceneGeom geom_of_particle(const SceneTable &T, int i) {
+    return T.count == 1 ? T.single : T.geom[scene_of(T.pbase, T.count, i)];
+}
+__device__ __forceinline__ SceneGeom geom_of_cell(const SceneTable &T, int c) {
+    return T.count == 1 ? T.single : T.geom[scene_of(T.cbase, T.count, c)];
+}
+
+// Scene of sorted particle i / of global cell c (the last scene whose range
+// starts at or before it; empty scenes are skipped by construction).
+__device__ __forceinline__ int scene_of(const int *base, int count, int i) {
+    if (count == 1) return 0;
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (base[mid] <= i)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
 
 // Device-resident counters of one frame (one 128-byte line).
 struct Counters {
@@ -73,9 +119,10 @@ struct Counters {
     int32_t pad[21];
 };
 
-// Per-frame device pointers of one scene.
+// Per-frame device pointers of one batch of scenes.
 struct Frame {
     int n;
+    SceneTable scenes;
     const float4 *pos_in, *vel_in, *ev_in;     // unsorted (previous order)
     float4 *pos, *vel, *ev, *acc;              // sorted (current order)
     uint32_t *key_in, *slot;                   // per source particle
@@ -123,6 +170,7 @@ void launch_checksum(const float4 *pos, int n, double *out5, cudaStream_t s);
 
 // Host-side helpers (scene.cpp).
 DevParams make_dev_params(const gsph_params &p);
+SceneGeom make_scene_geom(const gsph_params &p, int cbase);
 void set_error(const char *fmt, ...);
 
 }  // namespace gsph

@@ -56,7 +56,7 @@ __device__ __forceinline__ int slab_end(const Frame &f, int c, int s, int e,
 // Contiguous candidate range of one neighbour row: left cell from micro-x
 // `lo`, the middle cell, right cell up to micro-x `hi` (kernel_common.cuh:
 // 69-112 for TRA with lo = hi = own micro-x; 614-674 for SMS tasks).
-__device__ __forceinline__ void row_range(const Frame &f, const DevParams &P,
+__device__ __forceinline__ void row_range(const Frame &f, const SceneGeom &G,
                                           int m, int cx, int lo, int hi,
                                           int &begin, int &end) {
     const int sM = f.cell_start[m];
@@ -64,22 +64,23 @@ __device__ __forceinline__ void row_range(const Frame &f, const DevParams &P,
     begin = sM;
     end = eM;
     if (cx > 0) begin = slab_begin(f, m - 1, f.cell_start[m - 1], sM, lo);
-    if (cx + 1 < P.gx) end = slab_end(f, m + 1, eM, f.cell_start[m + 2], hi);
+    if (cx + 1 < G.gx) end = slab_end(f, m + 1, eM, f.cell_start[m + 2], hi);
 }
 
 struct MicroPos {
     int cx, cy, cz, lmx;
 };
 
-__device__ __forceinline__ MicroPos micro_of(float4 p, const DevParams &P) {
+__device__ __forceinline__ MicroPos micro_of(float4 p, const DevParams &P,
+                                             const SceneGeom &G) {
     // Same float arithmetic as the key (grid.cu); positions are inside the
     // grid after the arrange stage has clamped/flagged them.
     int mx = int(floorf(p.x * P.rat));
     int my = int(floorf(p.y * P.rat));
     int mz = int(floorf(p.z * P.rat));
-    mx = min(max(mx, 0), (P.gx << 2) - 1);
-    my = min(max(my, 0), (P.gy << 2) - 1);
-    mz = min(max(mz, 0), (P.gz << 2) - 1);
+    mx = min(max(mx, 0), (G.gx << 2) - 1);
+    my = min(max(my, 0), (G.gy << 2) - 1);
+    mz = min(max(mz, 0), (G.gz << 2) - 1);
     MicroPos r;
     r.cx = mx >> 2;
     r.cy = my >> 2;
@@ -215,7 +216,8 @@ k_density_tra(Frame f, DevParams P) {
         if (idx >= middle) continue;
         const int self = f.compact[idx];
         const float4 p = f.pos[self];
-        const MicroPos mp = micro_of(p, P);
+        const SceneGeom G = geom_of_particle(f.scenes, self);
+        const MicroPos mp = micro_of(p, P, G);
         uint32_t *masks = f.nbr_mask + size_t(u) * 9 * 32 + lane;
         int incomplete = 0;
         int found = 0;
@@ -224,10 +226,10 @@ k_density_tra(Frame f, DevParams P) {
             const int ny = mp.cy + (r % 3) - 1;
             const int nz = mp.cz + (r / 3) - 1;
             uint32_t mask = 0u;
-            if (ny >= 0 && ny < P.gy && nz >= 0 && nz < P.gz) {
-                const int m = mp.cx + P.gx * (ny + P.gy * nz);
+            if (ny >= 0 && ny < G.gy && nz >= 0 && nz < G.gz) {
+                const int m = G.cbase + mp.cx + G.gx * (ny + G.gy * nz);
                 int begin, end;
-                row_range(f, P, m, mp.cx, mp.lmx, mp.lmx, begin, end);
+                row_range(f, G, m, mp.cx, mp.lmx, mp.lmx, begin, end);
                 incomplete |= (end - begin > kMaskRowMax);
                 uint32_t bit = 1u;
 #pragma unroll 4
@@ -295,6 +297,7 @@ k_density_sms(Frame f, DevParams P) {
         const bool active = self < cend;
         if (cb + int(task.p_offset) >= cend) continue;   // warp-uniform
         const float4 p = f.pos[active ? self : cend - 1];
+        const SceneGeom G = geom_of_cell(f.scenes, task.cellid);
         const int cx = task.cell_pos[0], cy = task.cell_pos[1],
                   cz = task.cell_pos[2];
         const float2 npx = make_float2(-p.x, -p.x);
@@ -306,10 +309,10 @@ k_density_sms(Frame f, DevParams P) {
         for (int r = 0; r < 9; ++r) {
             const int ny = cy + (r % 3) - 1;
             const int nz = cz + (r / 3) - 1;
-            if (ny < 0 || ny >= P.gy || nz < 0 || nz >= P.gz) continue;
-            const int m = cx + P.gx * (ny + P.gy * nz);
+            if (ny < 0 || ny >= G.gy || nz < 0 || nz >= G.gz) continue;
+            const int m = G.cbase + cx + G.gx * (ny + G.gy * nz);
             int begin, end;
-            row_range(f, P, m, cx, task.xxi, task.xxx, begin, end);
+            row_range(f, G, m, cx, task.xxi, task.xxx, begin, end);
             for (int base = begin; base < end; base += kSmsBatch) {
                 const int cnt = min(kSmsBatch, end - base);
                 stage_xyz(f, base, cnt, sx, sy, sz, nullptr, nullptr, lane);
@@ -351,7 +354,8 @@ k_force_tra(Frame f, DevParams P, bool fresh) {
         const int self = f.compact[idx];
         const float4 p = f.pos[self];
         const float4 pev = f.ev[self];
-        const MicroPos mp = micro_of(p, P);
+        const SceneGeom G = geom_of_particle(f.scenes, self);
+        const MicroPos mp = micro_of(p, P, G);
         ForceAcc a = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         const int found = fresh ? f.nbr_flag[idx] : -1;
         if (found >= 0) {
@@ -362,7 +366,7 @@ k_force_tra(Frame f, DevParams P, bool fresh) {
                 if (mask) {
                     const int ny = mp.cy + (r % 3) - 1;
                     const int nz = mp.cz + (r / 3) - 1;
-                    const int m = mp.cx + P.gx * (ny + P.gy * nz);
+                    const int m = G.cbase + mp.cx + G.gx * (ny + G.gy * nz);
                     row_start[r][threadIdx.x] = mp.cx > 0
                         ? slab_begin(f, m - 1, f.cell_start[m - 1], f.cell_start[m], mp.lmx)
                         : f.cell_start[m];
@@ -385,10 +389,10 @@ k_force_tra(Frame f, DevParams P, bool fresh) {
             for (int r = 0; r < 9; ++r) {
                 const int ny = mp.cy + (r % 3) - 1;
                 const int nz = mp.cz + (r / 3) - 1;
-                if (ny < 0 || ny >= P.gy || nz < 0 || nz >= P.gz) continue;
-                const int m = mp.cx + P.gx * (ny + P.gy * nz);
+                if (ny < 0 || ny >= G.gy || nz < 0 || nz >= G.gz) continue;
+                const int m = G.cbase + mp.cx + G.gx * (ny + G.gy * nz);
                 int begin, end;
-                row_range(f, P, m, mp.cx, mp.lmx, mp.lmx, begin, end);
+                row_range(f, G, m, mp.cx, mp.lmx, mp.lmx, begin, end);
                 for (int j = begin; j < end; ++j) {
                     const float4 q = f.pos[j];
                     const float rx = p.x - q.x, ry = p.y - q.y, rz = p.z - q.z;
@@ -429,6 +433,7 @@ k_force_sms(Frame f, DevParams P) {
         const int safe = active ? self : cend - 1;
         const float4 p = f.pos[safe];
         const float4 pev = f.ev[safe];
+        const SceneGeom G = geom_of_cell(f.scenes, task.cellid);
         const int cx = task.cell_pos[0], cy = task.cell_pos[1],
                   cz = task.cell_pos[2];
         const float2 npx = make_float2(-p.x, -p.x);
@@ -450,10 +455,10 @@ k_force_sms(Frame f, DevParams P) {
         for (int r = 0; r < 9; ++r) {
             const int ny = cy + (r % 3) - 1;
             const int nz = cz + (r / 3) - 1;
-            if (ny < 0 || ny >= P.gy || nz < 0 || nz >= P.gz) continue;
-            const int m = cx + P.gx * (ny + P.gy * nz);
+            if (ny < 0 || ny >= G.gy || nz < 0 || nz >= G.gz) continue;
+            const int m = G.cbase + cx + G.gx * (ny + G.gy * nz);
             int begin, end;
-            row_range(f, P, m, cx, task.xxi, task.xxx, begin, end);
+            row_range(f, G, m, cx, task.xxi, task.xxx, begin, end);
             for (int base = begin; base < end; base += kSmsBatch) {
                 const int cnt = min(kSmsBatch, end - base);
 #pragma unroll
@@ -532,6 +537,7 @@ k_integrate(Frame f, DevParams P) {
     if (i >= f.n) return;
     const float4 tp = f.pos[i];
     const float4 ev = f.ev[i];
+    const SceneGeom G = geom_of_particle(f.scenes, i);
     const float4 v4 = f.vel[i];
     const float4 a4 = f.acc[i];
     float vx = v4.x, vy = v4.y, vz = v4.z;
@@ -540,17 +546,17 @@ k_integrate(Frame f, DevParams P) {
     const float beta = 200000.f;
     const float kernel = P.wall_kernel;
     float diff;
-    diff = kernel - (tp.y - P.bmin_y);
+    diff = kernel - (tp.y - P.bmin);
     if (diff > 0.0f) ay += alpha * diff - beta * vy;
-    diff = kernel - (P.bmax_y - tp.y);
+    diff = kernel - (G.bmax_y - tp.y);
     if (diff > 0.0f) ay -= alpha * diff + beta * vy;
-    diff = kernel - (tp.x - P.bmin_x);
+    diff = kernel - (tp.x - P.bmin);
     if (diff > 0.0f) ax += alpha * diff - beta * vx;
-    diff = kernel - (P.bmax_x - tp.x);
+    diff = kernel - (G.bmax_x - tp.x);
     if (diff > 0.0f) ax -= alpha * diff + beta * vx;
-    diff = kernel - (tp.z - P.bmin_z);
+    diff = kernel - (tp.z - P.bmin);
     if (diff > 0.0f) az += alpha * diff - beta * vz;
-    diff = kernel - (P.bmax_z - tp.z);
+    diff = kernel - (G.bmax_z - tp.z);
     if (diff > 0.0f) az -= alpha * diff + beta * vz;
     const float acc_limit = 3000000.f;
     const float vel_limit = 36.f;
@@ -577,12 +583,12 @@ k_integrate(Frame f, DevParams P) {
     float px = tp.x + vx * P.time_step;
     float py = tp.y + vy * P.time_step;
     float pz = tp.z + vz * P.time_step;
-    if (px >= P.bmax_x) { vx *= P.wall_damping; px = P.bmax_x - kernel; }
-    if (px <= P.bmin_x) { vx *= P.wall_damping; px = P.bmin_x + kernel; }
-    if (py >= P.bmax_y) { vy *= P.wall_damping; py = P.bmax_y - kernel; }
-    if (py <= P.bmin_y) { vy *= P.wall_damping; py = P.bmin_y + kernel; }
-    if (pz >= P.bmax_z) { vz *= P.wall_damping; pz = P.bmax_z - kernel; }
-    if (pz <= P.bmin_z) { vz *= P.wall_damping; pz = P.bmin_z + kernel; }
+    if (px >= G.bmax_x) { vx *= P.wall_damping; px = G.bmax_x - kernel; }
+    if (px <= P.bmin) { vx *= P.wall_damping; px = P.bmin + kernel; }
+    if (py >= G.bmax_y) { vy *= P.wall_damping; py = G.bmax_y - kernel; }
+    if (py <= P.bmin) { vy *= P.wall_damping; py = P.bmin + kernel; }
+    if (pz >= G.bmax_z) { vz *= P.wall_damping; pz = G.bmax_z - kernel; }
+    if (pz <= P.bmin) { vz *= P.wall_damping; pz = P.bmin + kernel; }
     f.pos[i] = make_float4(px, py, pz, tp.w);
     f.vel[i] = make_float4(vx, vy, vz, 0.f);
     f.ev[i] = make_float4((vx + ev.x) * 0.5f, (vy + ev.y) * 0.5f,

@@ -212,9 +212,6 @@ DevParams make_dev_params(const gsph_params &p) {
     d.h = p.kernel;
     d.h2 = p.kernel_2;
     d.rat = 4.f * p.inv_cell_size;   // sph_utils.cuh:48 "4.f * inv_cell_size"
-    d.gx = p.grid_size[0];
-    d.gy = p.grid_size[1];
-    d.gz = p.grid_size[2];
     d.numc = p.grid_size[0] * p.grid_size[1] * p.grid_size[2];
     d.density_scale = p.density_scale;
     d.self_density = p.self_density;
@@ -236,13 +233,20 @@ DevParams make_dev_params(const gsph_params &p) {
     d.gx_acc = p.gravity[0];
     d.gy_acc = p.gravity[1];
     d.gz_acc = p.gravity[2];
-    d.bmin_x = p.bound_min[0];
-    d.bmin_y = p.bound_min[1];
-    d.bmin_z = p.bound_min[2];
-    d.bmax_x = p.bound_max[0];
-    d.bmax_y = p.bound_max[1];
-    d.bmax_z = p.bound_max[2];
+    d.bmin = p.bound_min[0];
     return d;
+}
+
+SceneGeom make_scene_geom(const gsph_params &p, int cbase) {
+    SceneGeom g{};
+    g.gx = p.grid_size[0];
+    g.gy = p.grid_size[1];
+    g.gz = p.grid_size[2];
+    g.cbase = cbase;
+    g.bmax_x = p.bound_max[0];
+    g.bmax_y = p.bound_max[1];
+    g.bmax_z = p.bound_max[2];
+    return g;
 }
 
 }  // namespace gsph

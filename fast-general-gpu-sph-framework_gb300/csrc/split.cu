@@ -32,24 +32,26 @@ __device__ __forceinline__ int cell_n(const int32_t *__restrict__ start, int c) 
 // same neighbour bounds tests).
 __global__ void __launch_bounds__(256)
 k_cell_model(const int32_t *__restrict__ occ, const Counters *ctr,
-             const int32_t *__restrict__ start, DevParams P,
+             const int32_t *__restrict__ start, SceneTable T,
              int4 *__restrict__ val) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= ctr->num_occ) return;
-    const int idx = occ[k];
-    const int grid_x = P.gx, grid_y = P.gy;
+    const int gidx = occ[k];
+    const SceneGeom G = geom_of_cell(T, gidx);
+    const int idx = gidx - G.cbase;           // the scene's own cell index
+    const int grid_x = G.gx, grid_y = G.gy;
     const int slice = grid_x * grid_y;
-    const int numc = P.numc;
-    const int self = cell_n(start, idx);
+    const int numc = slice * G.gz;
+    const int self = cell_n(start, gidx);
     int totaln = self;
     const int x = idx % grid_x;
     const int y = (idx / grid_x) % grid_y;
-    if (x > 0) totaln += cell_n(start, idx - 1);
-    if (x + 1 < grid_x) totaln += cell_n(start, idx + 1);
-    if (y > 0) totaln += cell_n(start, idx - grid_x);
-    if (y + 1 < grid_y) totaln += cell_n(start, idx + grid_x);
-    if (idx >= slice) totaln += cell_n(start, idx - slice);
-    if (idx + slice < numc) totaln += cell_n(start, idx + slice);
+    if (x > 0) totaln += cell_n(start, gidx - 1);
+    if (x + 1 < grid_x) totaln += cell_n(start, gidx + 1);
+    if (y > 0) totaln += cell_n(start, gidx - grid_x);
+    if (y + 1 < grid_y) totaln += cell_n(start, gidx + grid_x);
+    if (idx >= slice) totaln += cell_n(start, gidx - slice);
+    if (idx + slice < numc) totaln += cell_n(start, gidx + slice);
     int req;
     if (totaln < 96 && self < 15)
         req = 0;
@@ -195,7 +197,7 @@ __global__ void __launch_bounds__(128)
 k_cell_emit(const int32_t *__restrict__ occ, const Counters *ctr,
             const int32_t *__restrict__ start, const uint32_t *__restrict__ key,
             const int4 *__restrict__ val, const int4 *__restrict__ prefix,
-            DevParams P, int32_t *__restrict__ compact,
+            SceneTable T, int32_t *__restrict__ compact,
             gsph_block_task *__restrict__ tasks) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= ctr->num_occ) return;
@@ -209,9 +211,11 @@ k_cell_emit(const int32_t *__restrict__ occ, const Counters *ctr,
     for (int j = 0; j < v.z; ++j) compact[pre.z + j] = b + v.y + j;
     for (int j = 0; j < v.y; ++j) compact[middle + pre.y + j] = b + j;
     if (v.x == 0) return;
-    const uint16_t cx = uint16_t(cell % P.gx);
-    const uint16_t cy = uint16_t(cell / P.gx % P.gy);
-    const uint16_t cz = uint16_t(cell / P.gx / P.gy);
+    const SceneGeom G = geom_of_cell(T, cell);
+    const int local = cell - G.cbase;
+    const uint16_t cx = uint16_t(local % G.gx);
+    const uint16_t cy = uint16_t(local / G.gx % G.gy);
+    const uint16_t cz = uint16_t(local / G.gx / G.gy);
     for (int t = 0; t < v.x; ++t) {
         const int ti = pre.x + t;
         if (ti >= task_count) break;   // capacity guard (error already raised)
@@ -301,8 +305,8 @@ void launch_split(const Frame &f, const DevParams &P, int max_occ,
                   cudaStream_t s) {
     if (f.n <= 0 || max_occ <= 0) return;
     const int blocks256 = (max_occ + 255) / 256;
-    k_cell_model<<<blocks256, 256, 0, s>>>(f.occ_list, f.ctr, f.cell_start, P,
-                                          f.cell_val);
+    k_cell_model<<<blocks256, 256, 0, s>>>(f.occ_list, f.ctr, f.cell_start,
+                                          f.scenes, f.cell_val);
     const int ntiles = (max_occ + kScanTile - 1) / kScanTile;
     k_val_scan_reduce<<<ntiles, kScanThreads, 0, s>>>(f.cell_val, f.ctr,
                                                      f.scan_tiles4);
@@ -311,8 +315,8 @@ void launch_split(const Frame &f, const DevParams &P, int max_occ,
     k_val_scan_apply<<<ntiles, kScanThreads, 0, s>>>(f.cell_val, f.ctr,
                                                     f.scan_tiles4, f.cell_prefix);
     k_cell_emit<<<(max_occ + 127) / 128, 128, 0, s>>>(
-        f.occ_list, f.ctr, f.cell_start, f.key, f.cell_val, f.cell_prefix, P,
-        f.compact, f.tasks);
+        f.occ_list, f.ctr, f.cell_start, f.key, f.cell_val, f.cell_prefix,
+        f.scenes, f.compact, f.tasks);
     const int max_pairs = (f.task_capacity + 1) / 2;
     k_judge<<<(max_pairs + 127) / 128, 128, 0, s>>>(f.tasks, f.ctr);
 }

@@ -122,21 +122,120 @@ struct System {
         return alloc(reinterpret_cast<void **>(p), count * sizeof(T));
     }
 
-    gsph_status init(const gsph_params &p, const float *pos4, const float *vel4,
-                     int count, int dev) {
-        params = p;
-        dp = make_dev_params(p);
+    // Scenes of the batch (a single scene is a batch of one).
+    std::vector<gsph_params> scene_params;
+    std::vector<int> pbase, cbase;          // [S + 1] particle / cell offsets
+    std::vector<SceneGeom> geom;            // [S]
+    SceneGeom *d_geom = nullptr;
+    int *d_pbase = nullptr, *d_cbase = nullptr;
+    int n_cap = 0, c_cap = 0, s_cap = 0;    // capacities of the buffers
+
+    // Every scene of a batch must share the physical parameters; only the box
+    // (world size, grid, upper walls) may differ.
+    static bool same_physics(const gsph_params &a, const gsph_params &b) {
+        gsph_params x = a, y = b;
+        for (gsph_params *q : {&x, &y}) {
+            for (int k = 0; k < 3; ++k) {
+                q->world_size[k] = 0.f;
+                q->grid_size[k] = 0;
+                q->bound_max[k] = 0.f;
+            }
+        }
+        return std::memcmp(&x, &y, sizeof(x)) == 0;
+    }
+
+    // Scene table for `count` scenes of the given sizes (host side).
+    gsph_status layout(const gsph_params *plist, const uint32_t *counts,
+                       int count, long long &n_total, long long &c_total) {
+        scene_params.assign(plist, plist + count);
+        pbase.assign(size_t(count) + 1, 0);
+        cbase.assign(size_t(count) + 1, 0);
+        geom.resize(size_t(count));
+        n_total = 0;
+        c_total = 0;
+        for (int k = 0; k < count; ++k) {
+            const gsph_params &q = plist[k];
+            if (!same_physics(q, plist[0])) {
+                set_error("scene %d of the batch has physical parameters that "
+                          "differ from scene 0 (only the box may differ)", k);
+                return GSPH_ERR_INVALID_ARG;
+            }
+            const long long cells =
+                (long long)q.grid_size[0] * q.grid_size[1] * q.grid_size[2];
+            if (cells <= 0) {
+                set_error("scene %d has an empty grid", k);
+                return GSPH_ERR_INVALID_ARG;
+            }
+            geom[size_t(k)] = make_scene_geom(q, int(c_total));
+            n_total += counts[k];
+            c_total += cells;
+            pbase[size_t(k) + 1] = int(std::min<long long>(n_total, 0x7FFFFFFF));
+            cbase[size_t(k) + 1] = int(std::min<long long>(c_total, 0x7FFFFFFF));
+        }
+        if (n_total > 0x7FFFFFFFLL) {
+            set_error("batch holds %lld particles; at most 2^31-1", n_total);
+            return GSPH_ERR_CAPACITY;
+        }
+        if (c_total >= 67108864LL) {   // 32-bit micro keys: cells * 64 < 2^32
+            set_error("batch holds %lld cells; at most 2^26", c_total);
+            return GSPH_ERR_CAPACITY;
+        }
+        return GSPH_OK;
+    }
+
+    gsph_status upload_table() {
+        const int S = int(geom.size());
+        GSPH_CUDA(cudaMemcpyAsync(d_geom, geom.data(), sizeof(SceneGeom) * S,
+                                  cudaMemcpyHostToDevice, stream));
+        GSPH_CUDA(cudaMemcpyAsync(d_pbase, pbase.data(), sizeof(int) * (S + 1),
+                                  cudaMemcpyHostToDevice, stream));
+        GSPH_CUDA(cudaMemcpyAsync(d_cbase, cbase.data(), sizeof(int) * (S + 1),
+                                  cudaMemcpyHostToDevice, stream));
+        fr.scenes.geom = d_geom;
+        fr.scenes.pbase = d_pbase;
+        fr.scenes.cbase = d_cbase;
+        fr.scenes.count = S;
+        fr.scenes.single = geom[0];
+        return GSPH_OK;
+    }
+
+    // Sizes that depend on the particle and cell counts of the current layout.
+    void set_counts(int n_particles, int n_cells) {
+        n = n_particles;
+        numc = n_cells;
+        dp.numc = n_cells;
+        max_occ = std::max(1, std::min(numc, n));
+        task_capacity = (n + kSmsTaskParticles - 1) / kSmsTaskParticles + max_occ + 2;
+        fr.n = n;
+        fr.task_capacity = task_capacity;
+        params = scene_params.empty() ? params : scene_params[0];
+        for (auto &g : graph)
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
+    }
+
+    gsph_status init(const gsph_params *plist, const uint32_t *counts, int count,
+                     const float *pos4, const float *vel4, int dev,
+                     long long n_capacity = 0, long long c_capacity = 0,
+                     int s_capacity = 0) {
         device = dev;
-        n = count;
-        numc = dp.numc;
         GSPH_CUDA(cudaSetDevice(device));
         num_sms = device_sm_count(device);
         GSPH_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-        max_occ = std::max(1, std::min(numc, n));
-        task_capacity = (n + kSmsTaskParticles - 1) / kSmsTaskParticles +
-                        max_occ + 2;
-        const size_t N = size_t(std::max(n, 1));
-        gsph_status st;
+        long long n_total = 0, c_total = 0;
+        gsph_status st = layout(plist, counts, count, n_total, c_total);
+        if (st) return st;
+        dp = make_dev_params(plist[0]);
+        params = plist[0];
+        n_cap = int(std::max<long long>(std::max(n_total, n_capacity), 1));
+        c_cap = int(std::max(c_total, c_capacity));
+        s_cap = std::max(count, s_capacity);
+        const int occ_cap = std::max(1, std::min(c_cap, n_cap));
+        const int task_cap =
+            (n_cap + kSmsTaskParticles - 1) / kSmsTaskParticles + occ_cap + 2;
+        const size_t N = size_t(n_cap), C = size_t(c_cap);
         for (int b = 0; b < 2; ++b) {
             if ((st = alloc_n(&pos[b], N)) || (st = alloc_n(&vel[b], N)) ||
                 (st = alloc_n(&ev[b], N)))
@@ -145,31 +244,32 @@ struct System {
         if ((st = alloc_n(&acc, N)) || (st = alloc_n(&fr.key_in, N)) ||
             (st = alloc_n(&fr.slot, N)) || (st = alloc_n(&fr.pairs, N)) ||
             (st = alloc_n(&fr.key, N)) || (st = alloc_n(&fr.perm, N)) ||
-            (st = alloc_n(&fr.cell_count, size_t(numc))) ||
-            (st = alloc_n(&fr.cell_start, size_t(numc) + 1)) ||
-            (st = alloc_n(&fr.cell_xslab, size_t(numc))) ||
-            (st = alloc_n(&fr.occ_list, size_t(max_occ))) ||
-            (st = alloc_n(&fr.big_list, size_t(max_occ))) ||
-            (st = alloc_n(&fr.cell_val, size_t(max_occ))) ||
-            (st = alloc_n(&fr.cell_prefix, size_t(max_occ))) ||
-            (st = alloc_n(&fr.tasks, size_t(task_capacity))) ||
+            (st = alloc_n(&fr.cell_count, C)) ||
+            (st = alloc_n(&fr.cell_start, C + 1)) ||
+            (st = alloc_n(&fr.cell_xslab, C)) ||
+            (st = alloc_n(&fr.occ_list, size_t(occ_cap))) ||
+            (st = alloc_n(&fr.big_list, size_t(occ_cap))) ||
+            (st = alloc_n(&fr.cell_val, size_t(occ_cap))) ||
+            (st = alloc_n(&fr.cell_prefix, size_t(occ_cap))) ||
+            (st = alloc_n(&fr.tasks, size_t(task_cap))) ||
             (st = alloc_n(&fr.compact, N)) ||
             (st = alloc_n(&fr.nbr_mask, ((N + 31) / 32) * 32 * 9)) ||
             (st = alloc_n(&fr.nbr_flag, N)) ||
-            (st = alloc_n(&fr.scan_tiles,
-                          size_t((numc + kScanTile - 1) / kScanTile))) ||
-            (st = alloc_n(&fr.scan_tiles4,
-                          size_t((max_occ + kScanTile - 1) / kScanTile))) ||
+            (st = alloc_n(&fr.scan_tiles, (C + kScanTile - 1) / kScanTile)) ||
+            (st = alloc_n(&fr.scan_tiles4, size_t((occ_cap + kScanTile - 1) / kScanTile))) ||
             (st = alloc_n(&fr.ctr, 1)) ||
-            (st = alloc_n(&red, size_t(8 + 8 * 512))))
+            (st = alloc_n(&red, size_t(8 + 8 * 512))) ||
+            (st = alloc_n(&d_geom, size_t(s_cap))) ||
+            (st = alloc_n(&d_pbase, size_t(s_cap) + 1)) ||
+            (st = alloc_n(&d_cbase, size_t(s_cap) + 1)))
             return st;
-        fr.n = n;
         fr.acc = acc;
-        fr.task_capacity = task_capacity;
-        GSPH_CUDA(cudaMemsetAsync(fr.cell_count, 0, sizeof(int32_t) * numc, stream));
-        GSPH_CUDA(cudaMemsetAsync(fr.cell_xslab, 0xFF, sizeof(uint32_t) * numc, stream));
+        set_counts(int(n_total), int(c_total));
+        if ((st = upload_table())) return st;
+        GSPH_CUDA(cudaMemsetAsync(fr.cell_count, 0, sizeof(int32_t) * C, stream));
+        GSPH_CUDA(cudaMemsetAsync(fr.cell_xslab, 0xFF, sizeof(uint32_t) * C, stream));
         GSPH_CUDA(cudaMemsetAsync(fr.ctr, 0, sizeof(Counters), stream));
-        GSPH_CUDA(cudaMemsetAsync(fr.tasks, 0, sizeof(gsph_block_task) * task_capacity, stream));
+        GSPH_CUDA(cudaMemsetAsync(fr.tasks, 0, sizeof(gsph_block_task) * task_cap, stream));
         for (int b = 0; b < 2; ++b) {
             GSPH_CUDA(cudaMemsetAsync(pos[b], 0, sizeof(float4) * N, stream));
             GSPH_CUDA(cudaMemsetAsync(vel[b], 0, sizeof(float4) * N, stream));
@@ -456,7 +556,8 @@ gsph_status gsph_create(const gsph_params *p, const float *pos4,
         set_error("gsph_create: host allocation failed");
         return GSPH_ERR_OUT_OF_MEMORY;
     }
-    gsph_status st = h->sys.init(*p, pos4, vel4, int(n), device);
+    const uint32_t counts[1] = {n};
+    gsph_status st = h->sys.init(p, counts, 1, pos4, vel4, device);
     if (st) {
         delete h;
         return st;
@@ -481,6 +582,66 @@ gsph_status gsph_create_from_json(const char *scene_path, int device,
     std::vector<float> pos(size_t(n) * 4 + 4);
     if ((st = gsph_lattice_fill(&sc, &p, pos.data(), n, &n))) return st;
     return gsph_create(&p, pos.data(), nullptr, n, device, out);
+}
+
+gsph_status gsph_batch_create(const gsph_params *params, const uint32_t *counts,
+                              uint32_t num_scenes, const float *pos4,
+                              const float *vel4, int device, gsph_handle *out) {
+    if (!params || !counts || !out || num_scenes == 0) {
+        set_error("gsph_batch_create: null argument or no scene");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    unsigned long long total = 0;
+    for (uint32_t k = 0; k < num_scenes; ++k) total += counts[k];
+    if (total > 0 && !pos4) {
+        set_error("gsph_batch_create: null positions");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    if (total > 0x7FFFFFFFull) {
+        set_error("gsph_batch_create: %llu particles exceed 2^31-1", total);
+        return GSPH_ERR_CAPACITY;
+    }
+    if (num_scenes > 1000000u) {
+        set_error("gsph_batch_create: too many scenes (%u)", num_scenes);
+        return GSPH_ERR_CAPACITY;
+    }
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        set_error("There is no CUDA device (%s).",
+                  e == cudaSuccess ? "count 0" : cudaGetErrorString(e));
+        return GSPH_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= count) {
+        set_error("device %d out of range [0, %d)", device, count);
+        return GSPH_ERR_INVALID_ARG;
+    }
+    gsph_system *h = new (std::nothrow) gsph_system();
+    if (!h) {
+        set_error("gsph_batch_create: host allocation failed");
+        return GSPH_ERR_OUT_OF_MEMORY;
+    }
+    gsph_status st = h->sys.init(params, counts, int(num_scenes), pos4, vel4, device);
+    if (st) {
+        delete h;
+        return st;
+    }
+    *out = h;
+    return GSPH_OK;
+}
+
+gsph_status gsph_batch_ranges(gsph_handle h, int32_t *pbase_out,
+                              int32_t *cbase_out) {
+    if (!h) {
+        set_error("null gsph handle");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    const System &s = h->sys;
+    if (pbase_out) std::copy(s.pbase.begin(), s.pbase.end(), pbase_out);
+    if (cbase_out) std::copy(s.cbase.begin(), s.cbase.end(), cbase_out);
+    return GSPH_OK;
 }
 
 gsph_status gsph_destroy(gsph_handle h) {
@@ -583,6 +744,7 @@ gsph_status gsph_get_info(gsph_handle h, gsph_info *out) {
     out->big_cells = c.num_big;
     out->frames = s.frames;
     out->device_bytes = s.device_bytes;
+    out->n_scenes = uint32_t(s.geom.size());
     return GSPH_OK;
 }
 
@@ -693,6 +855,66 @@ gsph_status gsph_copy_out(gsph_handle h, gsph_field field, void *host_dst,
         default: break;
     }
     set_error("gsph_copy_out: unsupported field %d", int(field));
+    return GSPH_ERR_INVALID_ARG;
+}
+
+gsph_status gsph_copy_out_scene(gsph_handle h, uint32_t scene, gsph_field field,
+                                void *host_dst, size_t bytes) {
+    gsph_status st = check_handle(h);
+    if (st) return st;
+    System &s = h->sys;
+    if (!host_dst || scene >= s.geom.size()) {
+        set_error("gsph_copy_out_scene: null destination or scene %u out of range",
+                  scene);
+        return GSPH_ERR_INVALID_ARG;
+    }
+    if ((st = s.sync_and_check()) && st != GSPH_ERR_DOMAIN) return st;
+    const int p0 = s.pbase[scene], p1 = s.pbase[scene + 1];
+    const int c0 = s.cbase[scene], c1 = s.cbase[scene + 1];
+    const size_t np = size_t(p1 - p0), nc = size_t(c1 - c0);
+    switch (field) {
+        case GSPH_FIELD_POSITION:
+        case GSPH_FIELD_VELOCITY:
+        case GSPH_FIELD_EVAL_VELOCITY:
+        case GSPH_FIELD_ACCELERATION: {
+            if (bytes != np * sizeof(float4)) break;
+            if (np)
+                GSPH_CUDA(cudaMemcpy(host_dst, state_ptr(s, field) + p0, bytes,
+                                     cudaMemcpyDeviceToHost));
+            return GSPH_OK;
+        }
+        case GSPH_FIELD_KEY:
+        case GSPH_FIELD_PERMUTATION: {
+            if (bytes != np * 4) break;
+            if (!np) return GSPH_OK;
+            const bool key = field == GSPH_FIELD_KEY;
+            GSPH_CUDA(cudaMemcpy(host_dst, key ? (const void *)(s.fr.key + p0)
+                                               : (const void *)(s.fr.perm + p0),
+                                 bytes, cudaMemcpyDeviceToHost));
+            uint32_t *o = static_cast<uint32_t *>(host_dst);
+            const uint32_t shift = key ? uint32_t(c0) << 6 : uint32_t(p0);
+            for (size_t i = 0; i < np; ++i) o[i] -= shift;
+            return GSPH_OK;
+        }
+        case GSPH_FIELD_CELL_START:
+        case GSPH_FIELD_CELL_COUNT: {
+            const bool start = field == GSPH_FIELD_CELL_START;
+            if (bytes != (start ? nc + 1 : nc) * 4) break;
+            std::vector<int32_t> st1(nc + 1);
+            GSPH_CUDA(cudaMemcpy(st1.data(), s.fr.cell_start + c0, (nc + 1) * 4,
+                                 cudaMemcpyDeviceToHost));
+            int32_t *o = static_cast<int32_t *>(host_dst);
+            for (size_t i = 0; i < nc; ++i)
+                o[i] = start ? st1[i] - p0 : st1[i + 1] - st1[i];
+            if (start) o[nc] = st1[nc] - p0;
+            return GSPH_OK;
+        }
+        default:
+            set_error("gsph_copy_out_scene: field %d has no per-scene form", int(field));
+            return GSPH_ERR_INVALID_ARG;
+    }
+    set_error("gsph_copy_out_scene: %zu bytes given for field %d of scene %u", bytes,
+              int(field), scene);
     return GSPH_ERR_INVALID_ARG;
 }
 
@@ -929,6 +1151,8 @@ gsph_status gsph_grid_sort_dev(const gsph_params *p, uint32_t n,
     };
     Frame f{};
     f.n = int(n);
+    f.scenes.count = 1;   // one scene: geometry passed inline, no device table
+    f.scenes.single = make_scene_geom(*p, 0);
     f.pos_in = reinterpret_cast<const float4 *>(pos_in);
     f.vel_in = reinterpret_cast<const float4 *>(vel_in);
     f.ev_in = reinterpret_cast<const float4 *>(ev_in);

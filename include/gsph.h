@@ -124,6 +124,8 @@ typedef struct {
     int32_t big_cells;           /* cells sorted by the block-level path */
     uint64_t frames;             /* ticks executed */
     uint64_t device_bytes;       /* device memory held by the handle */
+    uint32_t n_scenes;           /* scenes in the handle (1 unless batched) */
+    uint32_t reserved_;
 } gsph_info;
 
 /* Report of gsph_benchmark (the print block of runBenchmark,
@@ -180,6 +182,30 @@ gsph_status gsph_create(const gsph_params *p, const float *pos4,
 gsph_status gsph_create_from_json(const char *scene_path, int device,
                                   gsph_handle *out);
 gsph_status gsph_destroy(gsph_handle h);
+
+/* Batched step: num_scenes independent scenes stepped together, one launch
+ * per stage for all of them (segmented grid sort over the concatenated cell
+ * space, persistent density/force kernels over one work queue). params[k] is
+ * scene k's parameter set; all scenes must share the physical parameters and
+ * may differ in their box (world size, grid, walls). pos4/vel4 hold the
+ * scenes' particles one after another (counts[k] each, float4; vel4 may be
+ * NULL). Each scene evolves exactly as it would alone: same sort order, same
+ * neighbour order, same arithmetic (bit-identical results). The reference
+ * steps one scene per process and has no counterpart. */
+gsph_status gsph_batch_create(const gsph_params *params, const uint32_t *counts,
+                              uint32_t num_scenes, const float *pos4,
+                              const float *vel4, int device, gsph_handle *out);
+/* Particle and cell offsets of the scenes: pbase_out[num_scenes + 1],
+ * cbase_out[num_scenes + 1] (either may be NULL). Scene k's particles are
+ * rows [pbase[k], pbase[k+1]) of every particle field. */
+gsph_status gsph_batch_ranges(gsph_handle h, int32_t *pbase_out,
+                              int32_t *cbase_out);
+/* gsph_copy_out restricted to one scene, in that scene's own numbering
+ * (particle fields: the scene's rows; KEY: the scene's own micro keys;
+ * PERMUTATION: indices within the scene; CELL_START/CELL_COUNT: the scene's
+ * cells, offsets from its first particle). */
+gsph_status gsph_copy_out_scene(gsph_handle h, uint32_t scene, gsph_field field,
+                                void *host_dst, size_t bytes);
 
 /* One frame = arrange + density + force + advance (tick). */
 gsph_status gsph_step(gsph_handle h, int n_steps);
