@@ -19,6 +19,7 @@ path does not shard.
 from __future__ import annotations
 
 import argparse
+import collections
 import json
 import os
 import re
@@ -221,6 +222,267 @@ def run_reference(args, ws, rank):
     return 0
 
 
+def load_workloads():
+    import importlib.util
+    name = "gsph_gb300.workloads"
+    if name in sys.modules:
+        return sys.modules[name]
+    load_pkg()
+    spec = importlib.util.spec_from_file_location(
+        name, ROOT / "fast-general-gpu-sph-framework_gb300" / "workloads.py")
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def run_batched(args, ws, rank, local):
+    """Batched workload: independent dam-break scenes (N log-uniform in
+    [4,096, 262,144], column aspect uniform in [0.5, 2]) stepped as one batch
+    with CUDA graphs of `graph_frames` frames, against a loop over the same
+    scenes with the plain single-scene path."""
+    import torch
+    torch.cuda.set_device(local)
+    g = load_pkg()
+    W = load_workloads()
+    specs = W.batched_scenes(args.scenes, seed=rank)
+    scenes = [W.build(g, sp) for sp in specs]
+    total = sum(len(pos) for _, pos in scenes)
+    K = args.steps
+    b = g.Batch(scenes, device=local)
+    b.set_graph_mode(args.graph_frames)
+    b.step(args.warmup)
+    b.sync()
+    stream = torch.cuda.ExternalStream(b.stream(), device=torch.device("cuda", local))
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local)
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    t0 = time.perf_counter()
+    ev0.record(stream)
+    b.step(K)
+    ev1.record(stream)
+    ev1.synchronize()
+    wall_b = time.perf_counter() - t0
+    clk = clocks.stop()
+    dev_ms = ev0.elapsed_time(ev1)
+    info = b.info()
+    b.close()
+    batched = total * K / (dev_ms / 1e3)
+
+    def loop_rate(graph_frames):
+        hs = [g.HybridSystem(params=p, positions=pos, device=local) for p, pos in scenes]
+        for h in hs:
+            h.set_graph_mode(graph_frames)
+            h.step(args.warmup)
+            h.sync()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for h in hs:
+            h.step(K)
+            h.sync()
+        dt = time.perf_counter() - t
+        for h in hs:
+            h.close()
+        return total * K / dt, dt
+
+    loop_plain, t_plain = loop_rate(0)
+    loop_graph, t_graph = loop_rate(args.graph_frames)
+    line = {
+        "metric": "aggregate particle-steps/s, batched vs per-scene loop",
+        "value": batched, "unit": "particle-steps/s", "n_gpus": ws, "steps": K,
+        "warmup": args.warmup, "ms_per_step": dev_ms / K, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded jittered dam-break columns generated on the host",
+        "config": {"workload": f"batched: {len(scenes)} scenes, {total} particles, "
+                               f"N log-uniform [4096, 262144], aspect U[0.5, 2], "
+                               f"262k-scene physics, own boxes",
+                   "graph_frames": args.graph_frames, "cells": int(info.n_cells)},
+        "batched_wall_s": wall_b,
+        "per_scene_loop": {"value": loop_plain, "unit": "particle-steps/s",
+                           "wall_s": t_plain, "launch": "kernel by kernel"},
+        "per_scene_loop_graphs": {"value": loop_graph, "unit": "particle-steps/s",
+                                  "wall_s": t_graph,
+                                  "launch": f"CUDA graphs of {args.graph_frames} frames"},
+        "speedup_vs_loop": batched / loop_plain,
+        "speedup_vs_graph_loop": batched / loop_graph,
+        "clocks": clk,
+        "gpu_launches": LAUNCHES_PER_FRAME * K,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
+def load_serve():
+    import importlib.util
+    name = "gsph_gb300.serve"
+    if name in sys.modules:
+        return sys.modules[name]
+    load_pkg()
+    spec = importlib.util.spec_from_file_location(
+        name, ROOT / "fast-general-gpu-sph-framework_gb300" / "serve.py")
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def fifo_loop_model(g, W, trace, local, warmup):
+    """Per-scene FIFO loop of the plain path over the same trace: the frame
+    time of a single scene is measured at log-spaced sizes across the trace's
+    range (stream launches, state resident), interpolated in log-log for each
+    request, and the FIFO queue is replayed with service = K x frame time."""
+    sizes = sorted({(sp["nx"], sp["ny"], sp["nz"]) for _, sp, _ in trace},
+                   key=lambda s: s[0] * s[1] * s[2])
+    picks = [sizes[int(round(q * (len(sizes) - 1)))] for q in np.linspace(0, 1, 8)]
+    pts = []
+    for nx, ny, nz in dict.fromkeys(picks):
+        p, pos = W.build(g, {"nx": nx, "ny": ny, "nz": nz, "seed": 5})
+        with g.HybridSystem(params=p, positions=pos, device=local) as h:
+            h.step(warmup)
+            h.sync()
+            frames = max(10, min(200, int(2e8 / max(len(pos), 1))))
+            t = time.perf_counter()
+            h.step(frames)
+            h.sync()
+            pts.append((len(pos), (time.perf_counter() - t) / frames))
+    ln = np.log([n for n, _ in pts])
+    lt = np.log([t for _, t in pts])
+
+    def frame_s(n):
+        return float(np.exp(np.interp(np.log(n), ln, lt)))
+
+    free_at, lat, work = 0.0, [], 0.0
+    for t_arr, sp, k in trace:
+        n = sp["nx"] * sp["ny"] * sp["nz"]
+        start = max(free_at, t_arr)
+        free_at = start + k * frame_s(n)
+        lat.append(free_at - t_arr)
+        work += n * k
+    lat = np.array(lat)
+    return {"value": work / free_at, "unit": "particle-steps/s",
+            "p50_ms": float(np.percentile(lat, 50) * 1e3),
+            "p99_ms": float(np.percentile(lat, 99) * 1e3),
+            "makespan_s": free_at,
+            "frame_ms_at": {str(n): t * 1e3 for n, t in pts},
+            "method": "FIFO replay of the trace with service = K x measured "
+                      "single-scene frame time (8 sizes, log-log interpolation)"}
+
+
+def run_served(args, ws, rank, local):
+    """Served workload: Poisson arrivals (50/s) of dam-break requests (N
+    log-uniform in [8,192, 1,048,576], K uniform in [50, 500]) replayed in
+    real time. A client thread builds each scene when it arrives; the server
+    admits queued requests FIFO between chunks of frames while they fit the
+    HBM budget and the batch's capacity, steps all resident scenes together
+    and retires each after its K frames (its positions are read back)."""
+    import torch
+    torch.cuda.set_device(local)
+    g = load_pkg()
+    W = load_workloads()
+    S = load_serve()
+    trace = W.served_requests(args.duration, seed=1 + rank)
+    budget = int(args.budget_gb * 1e9)
+    # the batch's key space holds 2^26 global cells; particles sized to match
+    cap = (args.cap_particles, (1 << 26) - 1, 4096)
+    srv = S.SceneServer(g, budget_bytes=budget, capacity=cap, chunk=args.chunk,
+                        device=local, keep_results=False)
+    # warm the library (context, modules) on a small scene outside the timed run
+    p0, pos0 = W.build(g, {"nx": 16, "ny": 16, "nz": 16, "seed": 3})
+    with g.HybridSystem(params=p0, positions=pos0, device=local) as h:
+        h.step(args.warmup)
+        h.sync()
+
+    done_submitting = threading.Event()
+    t0 = time.perf_counter()
+    errors = []
+
+    def client():
+        # scenes are built up to 2 s ahead of their arrival by a small pool
+        # (the lattice fill releases the GIL) and submitted at arrival time
+        from concurrent.futures import ThreadPoolExecutor
+        ahead = collections.deque()
+        nxt = 0
+        try:
+            with ThreadPoolExecutor(max_workers=4) as pool:
+                for i, (t_arr, sp, k) in enumerate(trace):
+                    while nxt < len(trace) and trace[nxt][0] <= (
+                            time.perf_counter() - t0) + 2.0:
+                        ahead.append(pool.submit(W.build, g, trace[nxt][1]))
+                        nxt += 1
+                    if not ahead:
+                        ahead.append(pool.submit(W.build, g, sp))
+                        nxt += 1
+                    fut = ahead.popleft()
+                    dt = t0 + t_arr - time.perf_counter()
+                    if dt > 0:
+                        time.sleep(dt)
+                    p, pos = fut.result()
+                    srv.submit(S.Request(i, p, pos, k, t0 + t_arr))
+        except Exception as e:         # surfaced after the run
+            errors.append(e)
+        finally:
+            done_submitting.set()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    th = threading.Thread(target=client, daemon=True)
+    th.start()
+    busy = 0.0
+    peak_resident = 0
+    peak_particles = 0
+    while not (done_submitting.is_set() and not srv.queue and not srv.resident):
+        tb = time.perf_counter()
+        srv.admit()
+        if srv.resident:
+            peak_resident = max(peak_resident, len(srv.resident))
+            peak_particles = max(peak_particles, sum(r.n for r in srv.resident))
+            srv.step_chunk()
+            busy += time.perf_counter() - tb
+        else:
+            time.sleep(0.001)
+    makespan = time.perf_counter() - t0
+    clk = clocks.stop()
+    th.join()
+    srv.close()
+    if errors:
+        raise errors[0]
+    served = srv.particle_steps / makespan
+    lat = S.latency_stats(srv.done)
+    offered = sum(sp["nx"] * sp["ny"] * sp["nz"] * k for _, sp, k in trace)
+    loop = fifo_loop_model(g, W, trace, local, args.warmup)
+    line = {
+        "metric": "served aggregate particle-steps/s with p50/p99 completion latency",
+        "value": served, "unit": "particle-steps/s", "n_gpus": ws, "steps": srv.frames,
+        "warmup": args.warmup, "ms_per_step": srv.t_step * 1e3 / max(srv.frames, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded Poisson trace of jittered dam-break columns, "
+                "lattices built on arrival",
+        "config": {"workload": f"served: {len(trace)} requests over {args.duration:g} s "
+                               f"(Poisson 50/s), N log-uniform [8192, 1048576], "
+                               f"K uniform [50, 500]",
+                   "budget_gb": args.budget_gb, "capacity_particles": cap[0],
+                   "capacity_cells": cap[1], "chunk_frames": args.chunk},
+        "latency": lat,
+        "requests": len(srv.done), "offered_particle_steps": offered,
+        "makespan_s": makespan, "server_busy_s": busy,
+        "host_s": {"step_and_sync": srv.t_step, "repack": srv.t_repack,
+                   "readback": srv.t_readback, "chunks": srv.chunks},
+        "rejected": len(srv.rejected),
+        "peak_resident_scenes": peak_resident, "peak_resident_particles": peak_particles,
+        "per_scene_fifo_loop": loop,
+        "speedup_vs_loop": served / loop["value"],
+        "clocks": clk,
+        "gpu_launches": LAUNCHES_PER_FRAME * srv.frames + srv.chunks,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -231,10 +493,22 @@ def main():
     ap.add_argument("--no-e2e", action="store_true",
                     help="skip the end-to-end loop (profiling runs)")
     ap.add_argument("--scene", default=SCENE)
+    ap.add_argument("--workload", default="single", choices=["single", "batched", "served"])
+    ap.add_argument("--scenes", type=int, default=256, help="batched: scene count")
+    ap.add_argument("--graph-frames", type=int, default=10)
+    ap.add_argument("--duration", type=float, default=60.0, help="served: seconds of traffic")
+    ap.add_argument("--budget-gb", type=float, default=150.0, help="served: HBM state budget")
+    ap.add_argument("--cap-particles", type=int, default=40_000_000,
+                    help="served: particle capacity of the resident batch")
+    ap.add_argument("--chunk", type=int, default=10, help="served: frames between admissions")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, ws, rank)
+    if args.workload == "batched":
+        return run_batched(args, ws, rank, local)
+    if args.workload == "served":
+        return run_served(args, ws, rank, local)
 
     import torch
     dist = None

@@ -168,9 +168,17 @@ _SIGS = {
     "gsph_create": ([C.POINTER(Params), _VP, _VP, C.c_uint32, C.c_int, C.POINTER(_VP)], C.c_int),
     "gsph_create_from_json": ([C.c_char_p, C.c_int, C.POINTER(_VP)], C.c_int),
     "gsph_destroy": ([_VP], C.c_int),
+    "gsph_snapshot_save": ([_VP, C.c_char_p], C.c_int),
+    "gsph_snapshot_load": ([C.c_char_p, C.c_int, C.POINTER(_VP)], C.c_int),
+    "gsph_snapshot_info": ([C.c_char_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint64),
+                            C.POINTER(C.c_uint64)], C.c_int),
     "gsph_batch_create": ([C.POINTER(Params), C.POINTER(C.c_uint32), C.c_uint32, _VP, _VP,
                            C.c_int, C.POINTER(_VP)], C.c_int),
     "gsph_batch_ranges": ([_VP, _VP, _VP], C.c_int),
+    "gsph_batch_create_ex": ([C.POINTER(Params), C.POINTER(C.c_uint32), C.c_uint32, _VP, _VP,
+                              C.c_uint64, C.c_uint64, C.c_uint32, C.c_int, C.POINTER(_VP)],
+                             C.c_int),
+    "gsph_batch_repack": ([_VP, _VP, C.c_uint32, _VP, _VP, C.c_uint32, _VP, _VP], C.c_int),
     "gsph_copy_out_scene": ([_VP, C.c_uint32, C.c_int, _VP, C.c_size_t], C.c_int),
     "gsph_step": ([_VP, C.c_int], C.c_int),
     "gsph_arrange": ([_VP], C.c_int),
@@ -355,8 +363,10 @@ class HybridSystem:
     def copy_out_async(self, field: int, host_ptr: int, nbytes: int) -> None:
         _check(self._lib.gsph_copy_out_async(self._h, field, host_ptr, nbytes))
 
-    def set_graph_mode(self, on: bool) -> None:
-        _check(self._lib.gsph_set_graph_mode(self._h, int(bool(on))))
+    def set_graph_mode(self, frames) -> None:
+        """frames > 0: step through CUDA graphs of that many frames; 0 or
+        False: launch kernel by kernel (True means one frame per graph)."""
+        _check(self._lib.gsph_set_graph_mode(self._h, int(frames)))
 
     def set_stage_timing(self, on: bool) -> None:
         _check(self._lib.gsph_set_stage_timing(self._h, int(bool(on))))
@@ -421,6 +431,10 @@ class HybridSystem:
         keys = ("mass", "px", "py", "pz", "kinetic", "sx", "sy", "sz")
         return dict(zip(keys, out))
 
+    def save_snapshot(self, path: os.PathLike | str) -> None:
+        """gsph_snapshot_save: the state, parameters and frame counter."""
+        _check(self._lib.gsph_snapshot_save(self._h, str(path).encode()))
+
     def runBenchmark(self, frames: int) -> dict:
         r = BenchReport()
         _check(self._lib.gsph_benchmark(self._h, frames, C.byref(r)))
@@ -433,17 +447,72 @@ class HybridSystem:
         return self._h.value
 
 
+def snapshot_info(path: os.PathLike | str) -> dict:
+    """Header of a snapshot file: scenes, particles, frames."""
+    s, n, f = C.c_uint32(), C.c_uint64(), C.c_uint64()
+    _check(load_library().gsph_snapshot_info(str(path).encode(), C.byref(s), C.byref(n),
+                                             C.byref(f)))
+    return {"n_scenes": s.value, "n_particles": n.value, "frames": f.value}
+
+
+def load_snapshot(path: os.PathLike | str, device: int = 0):
+    """gsph_snapshot_load: a HybridSystem (one scene) or a Batch that
+    continues the saved run bit for bit."""
+    lib = load_library()
+    h = C.c_void_p()
+    _check(lib.gsph_snapshot_load(str(path).encode(), device, C.byref(h)))
+    info = Info()
+    st = lib.gsph_get_info(h, C.byref(info))
+    if st:
+        lib.gsph_destroy(h)
+        _check(st)
+    cls = Batch if info.n_scenes > 1 else HybridSystem
+    obj = cls.__new__(cls)
+    obj._h = h
+    obj._lib = lib
+    obj.params = Params()
+    _check(lib.gsph_get_params(h, C.byref(obj.params)))
+    if cls is Batch:
+        obj._refresh()
+    else:
+        obj.n = int(info.n_particles)
+    return obj
+
+
 class Batch(HybridSystem):
     """Several independent scenes stepped together (gsph_batch_create): one
     launch per stage for all of them. Scene k evolves exactly as it would
     alone (bit-identical). `scenes` is a list of (params, positions[,
     velocities]) with a common physical parameter set."""
 
-    def __init__(self, scenes, device: int = 0):
+    def __init__(self, scenes, device: int = 0, capacity=None):
+        """capacity: optional (particles, cells, scenes) to reserve for
+        repack(); by default the buffers fit the initial scenes exactly."""
         lib = load_library()
+        plist, counts, pos_all, vel_all = self._pack(scenes)
+        h = C.c_void_p()
+        if capacity is None:
+            _check(lib.gsph_batch_create(plist, counts, len(scenes),
+                                         _ptr(pos_all) if len(pos_all) else None,
+                                         _ptr(vel_all) if len(vel_all) else None,
+                                         device, C.byref(h)))
+        else:
+            pc, cc, sc = capacity
+            _check(lib.gsph_batch_create_ex(plist, counts, len(scenes),
+                                            _ptr(pos_all) if len(pos_all) else None,
+                                            _ptr(vel_all) if len(vel_all) else None,
+                                            int(pc), int(cc), int(sc), device, C.byref(h)))
+        self._h = h
+        self._lib = lib
+        self.params = Params()
+        _check(lib.gsph_get_params(h, C.byref(self.params)))
+        self._refresh()
+
+    @staticmethod
+    def _pack(scenes):
         S = len(scenes)
-        plist = (Params * S)()
-        counts = (C.c_uint32 * S)()
+        plist = (Params * max(S, 1))()
+        counts = (C.c_uint32 * max(S, 1))()
         pos_parts, vel_parts = [], []
         for k, sc in enumerate(scenes):
             p, pos = sc[0], np.ascontiguousarray(sc[1], np.float32).reshape(-1, 4)
@@ -455,20 +524,26 @@ class Batch(HybridSystem):
             vel_parts.append(vel)
         pos_all = np.concatenate(pos_parts) if pos_parts else np.zeros((0, 4), np.float32)
         vel_all = np.concatenate(vel_parts) if vel_parts else np.zeros((0, 4), np.float32)
-        h = C.c_void_p()
-        _check(lib.gsph_batch_create(plist, counts, S,
-                                     _ptr(pos_all) if len(pos_all) else None,
-                                     _ptr(vel_all) if len(vel_all) else None,
-                                     device, C.byref(h)))
-        self._h = h
-        self._lib = lib
-        self.params = Params()
-        _check(lib.gsph_get_params(h, C.byref(self.params)))
-        self.n = int(self.info().n_particles)
-        self.num_scenes = S
+        return plist, counts, np.ascontiguousarray(pos_all), np.ascontiguousarray(vel_all)
+
+    def _refresh(self):
+        info = self.info()
+        self.n = int(info.n_particles)
+        self.num_scenes = S = int(info.n_scenes)
         self.pbase = np.empty(S + 1, np.int32)
         self.cbase = np.empty(S + 1, np.int32)
-        _check(lib.gsph_batch_ranges(h, _ptr(self.pbase), _ptr(self.cbase)))
+        _check(self._lib.gsph_batch_ranges(self._h, _ptr(self.pbase), _ptr(self.cbase)))
+
+    def repack(self, keep, add_scenes=()) -> None:
+        """Keep the listed scenes (in that order), then append add_scenes."""
+        keep_a = np.ascontiguousarray(keep, np.uint32)
+        plist, counts, pos_all, vel_all = self._pack(list(add_scenes))
+        _check(self._lib.gsph_batch_repack(
+            self._h, _ptr(keep_a) if len(keep_a) else None, len(keep_a),
+            plist, counts, len(add_scenes),
+            _ptr(pos_all) if len(pos_all) else None,
+            _ptr(vel_all) if len(vel_all) else None))
+        self._refresh()
 
     def copy_out_scene(self, scene: int, field: int) -> np.ndarray:
         n = int(self.pbase[scene + 1] - self.pbase[scene])

@@ -12,6 +12,7 @@
 #define GSPH_INTERNAL_H_
 
 #include <cstdint>
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "../../include/gsph.h"
@@ -172,6 +173,18 @@ void launch_checksum(const float4 *pos, int n, double *out5, cudaStream_t s);
 DevParams make_dev_params(const gsph_params &p);
 SceneGeom make_scene_geom(const gsph_params &p, int cbase);
 void set_error(const char *fmt, ...);
+
+// Snapshot file format (snapshot.cpp).
+gsph_status snapshot_write(const char *path, const gsph_params *plist,
+                           const uint32_t *counts, uint32_t n_scenes,
+                           const float *pos4, const float *vel4, const float *ev4,
+                           uint64_t frames);
+gsph_status snapshot_header(const char *path, uint32_t *n_scenes,
+                            uint64_t *n_particles, uint64_t *frames);
+gsph_status snapshot_read(const char *path, std::vector<gsph_params> &plist,
+                          std::vector<uint32_t> &counts, std::vector<float> &pos4,
+                          std::vector<float> &vel4, std::vector<float> &ev4,
+                          uint64_t &frames);
 
 }  // namespace gsph
 

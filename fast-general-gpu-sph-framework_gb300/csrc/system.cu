@@ -47,6 +47,33 @@ int device_sm_count(int device) {
     return v;
 }
 
+// Repack: gathers the kept scenes' particle state into the front of the
+// other buffer set. Kept scene k moves from [src_base[k], +count) to
+// [dst_base[k], dst_base[k+1]); one thread per destination particle finds
+// its scene by binary search over dst_base (empty scenes are skipped by
+// taking the last base <= i).
+__global__ void __launch_bounds__(256)
+k_repack_gather(const float4 *__restrict__ pos_s, const float4 *__restrict__ vel_s,
+                const float4 *__restrict__ ev_s, float4 *__restrict__ pos_d,
+                float4 *__restrict__ vel_d, float4 *__restrict__ ev_d,
+                const int *__restrict__ dst_base, const int *__restrict__ src_base,
+                int n_keep, int total) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    int lo = 0, hi = n_keep - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (dst_base[mid] <= i)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    const int src = src_base[lo] + (i - dst_base[lo]);
+    pos_d[i] = pos_s[src];
+    vel_d[i] = vel_s[src];
+    ev_d[i] = ev_s[src];
+}
+
 }  // namespace
 
 struct System {
@@ -73,8 +100,8 @@ struct System {
     bool lists_valid = false;   // TRA neighbour masks match the state
     uint64_t frames = 0;
 
-    bool graph_mode = false;
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int graph_frames = 0;   // frames per captured CUDA graph (0: stream launches)
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};   // by starting parity
 
     bool timing = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -128,6 +155,7 @@ struct System {
     std::vector<SceneGeom> geom;            // [S]
     SceneGeom *d_geom = nullptr;
     int *d_pbase = nullptr, *d_cbase = nullptr;
+    int *d_repack = nullptr;   // repack gather table: dst bases, src bases
     int n_cap = 0, c_cap = 0, s_cap = 0;    // capacities of the buffers
 
     // Every scene of a batch must share the physical parameters; only the box
@@ -185,6 +213,10 @@ struct System {
 
     gsph_status upload_table() {
         const int S = int(geom.size());
+        if (S > s_cap) {
+            set_error("batch of %d scenes exceeds its capacity of %d", S, s_cap);
+            return GSPH_ERR_CAPACITY;
+        }
         GSPH_CUDA(cudaMemcpyAsync(d_geom, geom.data(), sizeof(SceneGeom) * S,
                                   cudaMemcpyHostToDevice, stream));
         GSPH_CUDA(cudaMemcpyAsync(d_pbase, pbase.data(), sizeof(int) * (S + 1),
@@ -195,7 +227,7 @@ struct System {
         fr.scenes.pbase = d_pbase;
         fr.scenes.cbase = d_cbase;
         fr.scenes.count = S;
-        fr.scenes.single = geom[0];
+        if (S > 0) fr.scenes.single = geom[0];
         return GSPH_OK;
     }
 
@@ -209,11 +241,7 @@ struct System {
         fr.n = n;
         fr.task_capacity = task_capacity;
         params = scene_params.empty() ? params : scene_params[0];
-        for (auto &g : graph)
-            if (g) {
-                cudaGraphExecDestroy(g);
-                g = nullptr;
-            }
+        drop_graphs();
     }
 
     gsph_status init(const gsph_params *plist, const uint32_t *counts, int count,
@@ -225,6 +253,10 @@ struct System {
         num_sms = device_sm_count(device);
         GSPH_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         long long n_total = 0, c_total = 0;
+        if (count < 1) {
+            set_error("a batch needs at least one scene at creation");
+            return GSPH_ERR_INVALID_ARG;
+        }
         gsph_status st = layout(plist, counts, count, n_total, c_total);
         if (st) return st;
         dp = make_dev_params(plist[0]);
@@ -261,7 +293,8 @@ struct System {
             (st = alloc_n(&red, size_t(8 + 8 * 512))) ||
             (st = alloc_n(&d_geom, size_t(s_cap))) ||
             (st = alloc_n(&d_pbase, size_t(s_cap) + 1)) ||
-            (st = alloc_n(&d_cbase, size_t(s_cap) + 1)))
+            (st = alloc_n(&d_cbase, size_t(s_cap) + 1)) ||
+            (st = alloc_n(&d_repack, 2 * size_t(s_cap) + 2)))
             return st;
         fr.acc = acc;
         set_counts(int(n_total), int(c_total));
@@ -284,6 +317,103 @@ struct System {
                                           cudaMemcpyHostToDevice, stream));
         }
         cur = 0;
+        GSPH_CUDA(cudaStreamSynchronize(stream));
+        return GSPH_OK;
+    }
+
+    // New scene set: the kept scenes (by current index, in the given order)
+    // followed by new ones. The kept scenes' state is copied on the device
+    // in its current order, so each continues exactly as if alone.
+    gsph_status repack(const uint32_t *keep, int n_keep, const gsph_params *add_p,
+                       const uint32_t *add_n, int n_add, const float *add_pos4,
+                       const float *add_vel4) {
+        const int S_old = int(geom.size());
+        std::vector<gsph_params> plist;
+        std::vector<uint32_t> counts;
+        std::vector<int> src_base;
+        for (int k = 0; k < n_keep; ++k) {
+            if (keep[k] >= uint32_t(S_old)) {
+                set_error("repack: scene %u out of range", keep[k]);
+                return GSPH_ERR_INVALID_ARG;
+            }
+            plist.push_back(scene_params[keep[k]]);
+            counts.push_back(uint32_t(pbase[keep[k] + 1] - pbase[keep[k]]));
+            src_base.push_back(pbase[keep[k]]);
+        }
+        for (int k = 0; k < n_add; ++k) {
+            plist.push_back(add_p[k]);
+            counts.push_back(add_n[k]);
+        }
+        const int S = n_keep + n_add;
+        if (S > 0 && !same_physics(plist[0], params)) {
+            set_error("repack: new scenes must share the batch's physical parameters");
+            return GSPH_ERR_INVALID_ARG;
+        }
+        if (S > s_cap) {
+            set_error("repack: %d scenes exceed the capacity of %d", S, s_cap);
+            return GSPH_ERR_CAPACITY;
+        }
+        // validate before touching any state
+        std::vector<gsph_params> old_params = scene_params;
+        std::vector<int> old_pbase = pbase, old_cbase = cbase;
+        std::vector<SceneGeom> old_geom = geom;
+        long long n_total = 0, c_total = 0;
+        gsph_status st = S > 0 ? layout(plist.data(), counts.data(), S, n_total, c_total)
+                               : GSPH_OK;
+        if (st == GSPH_OK && (n_total > n_cap || c_total > c_cap)) {
+            set_error("repack: %lld particles / %lld cells exceed the capacity "
+                      "(%d / %d)", n_total, c_total, n_cap, c_cap);
+            st = GSPH_ERR_CAPACITY;
+        }
+        if (st) {
+            scene_params = old_params;
+            pbase = old_pbase;
+            cbase = old_cbase;
+            geom = old_geom;
+            return st;
+        }
+        if (S == 0) {
+            scene_params.clear();
+            pbase.assign(1, 0);
+            cbase.assign(1, 0);
+            geom.clear();
+        }
+        const int dst = 1 - cur;
+        // kept scenes: one gather launch into the front of the other buffers
+        const int kept_total = n_keep > 0 ? pbase[size_t(n_keep)] : 0;
+        if (kept_total > 0) {
+            std::vector<int> table(size_t(2 * n_keep + 1));
+            for (int k = 0; k <= n_keep; ++k) table[size_t(k)] = pbase[size_t(k)];
+            for (int k = 0; k < n_keep; ++k)
+                table[size_t(n_keep + 1 + k)] = src_base[size_t(k)];
+            GSPH_CUDA(cudaMemcpyAsync(d_repack, table.data(), sizeof(int) * table.size(),
+                                      cudaMemcpyHostToDevice, stream));
+            k_repack_gather<<<(kept_total + 255) / 256, 256, 0, stream>>>(
+                pos[cur], vel[cur], ev[cur], pos[dst], vel[dst], ev[dst], d_repack,
+                d_repack + n_keep + 1, n_keep, kept_total);
+            GSPH_CUDA(cudaGetLastError());
+        }
+        // new scenes: contiguous after the kept ones, one copy per array
+        const size_t added = size_t(n_total - kept_total);
+        if (added > 0) {
+            GSPH_CUDA(cudaMemcpyAsync(pos[dst] + kept_total, add_pos4,
+                                      sizeof(float4) * added, cudaMemcpyHostToDevice,
+                                      stream));
+            if (add_vel4)
+                GSPH_CUDA(cudaMemcpyAsync(vel[dst] + kept_total, add_vel4,
+                                          sizeof(float4) * added,
+                                          cudaMemcpyHostToDevice, stream));
+            else
+                GSPH_CUDA(cudaMemsetAsync(vel[dst] + kept_total, 0,
+                                          sizeof(float4) * added, stream));
+            GSPH_CUDA(cudaMemsetAsync(ev[dst] + kept_total, 0, sizeof(float4) * added,
+                                      stream));
+        }
+        cur = dst;
+        set_counts(int(n_total), int(c_total));
+        if ((st = upload_table())) return st;
+        arranged = false;
+        lists_valid = false;
         GSPH_CUDA(cudaStreamSynchronize(stream));
         return GSPH_OK;
     }
@@ -352,13 +482,18 @@ struct System {
         return e;
     }
 
+    // Capture graph_frames whole frames starting from buffer `parity`.
     gsph_status build_graph(int parity) {
         cudaGraph_t g = nullptr;
         GSPH_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-        enqueue_arrange(parity);
-        enqueue_density(1 - parity);
-        enqueue_force(1 - parity);
-        enqueue_advance(1 - parity);
+        int in = parity;
+        for (int k = 0; k < graph_frames; ++k) {
+            enqueue_arrange(in);
+            enqueue_density(1 - in);
+            enqueue_force(1 - in);
+            enqueue_advance(1 - in);
+            in = 1 - in;
+        }
         cudaError_t e = cudaStreamEndCapture(stream, &g);
         if (e != cudaSuccess) {
             set_error("graph capture failed: %s", cudaGetErrorString(e));
@@ -375,37 +510,63 @@ struct System {
         return GSPH_OK;
     }
 
+    void drop_graphs() {
+        for (auto &g : graph)
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
+    }
+
+    // One frame launched kernel by kernel (with stage events when timing).
     gsph_status tick() {
+        if (numc == 0) return GSPH_OK;   // a batch without scenes
         const int in = cur, out = 1 - cur;
-        if (graph_mode && !timing) {
-            if (!graph[in]) {
-                gsph_status st = build_graph(in);
-                if (st) return st;
-            }
-            GSPH_CUDA(cudaGraphLaunch(graph[in], stream));
-        } else {
-            std::vector<cudaEvent_t> evs;
-            if (timing) {
-                for (int k = 0; k < 5; ++k) evs.push_back(take_event());
-                cudaEventRecord(evs[0], stream);
-            }
-            enqueue_arrange(in);
-            if (timing) cudaEventRecord(evs[1], stream);
-            enqueue_density(out);
-            if (timing) cudaEventRecord(evs[2], stream);
-            enqueue_force(out);
-            if (timing) cudaEventRecord(evs[3], stream);
-            enqueue_advance(out);
-            if (timing) {
-                cudaEventRecord(evs[4], stream);
-                ev_pending.push_back(std::move(evs));
-            }
-            gsph_status st = check_launch();
-            if (st) return st;
+        std::vector<cudaEvent_t> evs;
+        if (timing) {
+            for (int k = 0; k < 5; ++k) evs.push_back(take_event());
+            cudaEventRecord(evs[0], stream);
         }
+        enqueue_arrange(in);
+        if (timing) cudaEventRecord(evs[1], stream);
+        enqueue_density(out);
+        if (timing) cudaEventRecord(evs[2], stream);
+        enqueue_force(out);
+        if (timing) cudaEventRecord(evs[3], stream);
+        enqueue_advance(out);
+        if (timing) {
+            cudaEventRecord(evs[4], stream);
+            ev_pending.push_back(std::move(evs));
+        }
+        gsph_status st = check_launch();
+        if (st) return st;
         cur = out;
         arranged = true;
         ++frames;
+        return GSPH_OK;
+    }
+
+    // n frames: whole captured graphs while they fit, single frames after.
+    gsph_status step(int n) {
+        if (numc == 0) return GSPH_OK;   // a batch without scenes
+        if (graph_frames > 0 && !timing) {
+            while (n >= graph_frames) {
+                if (!graph[cur]) {
+                    gsph_status st = build_graph(cur);
+                    if (st) return st;
+                }
+                GSPH_CUDA(cudaGraphLaunch(graph[cur], stream));
+                if (graph_frames & 1) cur = 1 - cur;
+                arranged = true;
+                lists_valid = false;
+                frames += uint64_t(graph_frames);
+                n -= graph_frames;
+            }
+        }
+        for (int k = 0; k < n; ++k) {
+            gsph_status st = tick();
+            if (st) return st;
+        }
         return GSPH_OK;
     }
 
@@ -644,6 +805,69 @@ gsph_status gsph_batch_ranges(gsph_handle h, int32_t *pbase_out,
     return GSPH_OK;
 }
 
+gsph_status gsph_batch_create_ex(const gsph_params *params, const uint32_t *counts,
+                                 uint32_t num_scenes, const float *pos4,
+                                 const float *vel4, uint64_t particle_capacity,
+                                 uint64_t cell_capacity, uint32_t scene_capacity,
+                                 int device, gsph_handle *out) {
+    if (!params || !counts || !out || num_scenes == 0) {
+        set_error("gsph_batch_create_ex: null argument or no scene");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    if (particle_capacity > 0x7FFFFFFFull || cell_capacity >= 67108864ull ||
+        scene_capacity > 1000000u) {
+        set_error("gsph_batch_create_ex: capacity out of range");
+        return GSPH_ERR_CAPACITY;
+    }
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        set_error("There is no CUDA device.");
+        return GSPH_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= count) {
+        set_error("device %d out of range [0, %d)", device, count);
+        return GSPH_ERR_INVALID_ARG;
+    }
+    gsph_system *h = new (std::nothrow) gsph_system();
+    if (!h) {
+        set_error("gsph_batch_create_ex: host allocation failed");
+        return GSPH_ERR_OUT_OF_MEMORY;
+    }
+    gsph_status st = h->sys.init(params, counts, int(num_scenes), pos4, vel4, device,
+                                 (long long)particle_capacity, (long long)cell_capacity,
+                                 int(scene_capacity));
+    if (st) {
+        delete h;
+        return st;
+    }
+    *out = h;
+    return GSPH_OK;
+}
+
+gsph_status gsph_batch_repack(gsph_handle h, const uint32_t *keep, uint32_t n_keep,
+                              const gsph_params *add_params, const uint32_t *add_counts,
+                              uint32_t n_add, const float *add_pos4,
+                              const float *add_vel4) {
+    gsph_status st = check_handle(h);
+    if (st) return st;
+    if ((n_keep && !keep) || (n_add && (!add_params || !add_counts))) {
+        set_error("gsph_batch_repack: null argument");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    unsigned long long added = 0;
+    for (uint32_t k = 0; k < n_add; ++k) added += add_counts[k];
+    if (added && !add_pos4) {
+        set_error("gsph_batch_repack: null positions");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    System &s = h->sys;
+    GSPH_CUDA(cudaStreamSynchronize(s.stream));
+    return s.repack(keep, int(n_keep), add_params, add_counts, int(n_add), add_pos4,
+                    add_vel4);
+}
+
 gsph_status gsph_destroy(gsph_handle h) {
     if (!h) return GSPH_OK;
     delete h;
@@ -657,9 +881,7 @@ gsph_status gsph_step(gsph_handle h, int n_steps) {
         set_error("gsph_step: negative step count");
         return GSPH_ERR_INVALID_ARG;
     }
-    for (int i = 0; i < n_steps; ++i)
-        if ((st = h->sys.tick())) return st;
-    return GSPH_OK;
+    return h->sys.step(n_steps);
 }
 
 gsph_status gsph_arrange(gsph_handle h) {
@@ -705,7 +927,12 @@ gsph_status gsph_advance(gsph_handle h) {
 gsph_status gsph_set_graph_mode(gsph_handle h, int enabled) {
     gsph_status st = check_handle(h);
     if (st) return st;
-    h->sys.graph_mode = enabled != 0;
+    if (enabled < 0) {
+        set_error("gsph_set_graph_mode: negative frame count");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    if (enabled != h->sys.graph_frames) h->sys.drop_graphs();
+    h->sys.graph_frames = enabled;
     return GSPH_OK;
 }
 
@@ -973,6 +1200,68 @@ gsph_status gsph_copy_out_async(gsph_handle h, gsph_field field, void *host_dst,
     return GSPH_OK;
 }
 
+gsph_status gsph_snapshot_save(gsph_handle h, const char *path) {
+    gsph_status st = check_handle(h);
+    if (st) return st;
+    System &s = h->sys;
+    GSPH_CUDA(cudaStreamSynchronize(s.stream));
+    const size_t n = size_t(s.n);
+    std::vector<float> pos(n * 4), vel(n * 4), ev(n * 4);
+    if (n) {
+        GSPH_CUDA(cudaMemcpy(pos.data(), s.pos[s.cur], n * 16, cudaMemcpyDeviceToHost));
+        GSPH_CUDA(cudaMemcpy(vel.data(), s.vel[s.cur], n * 16, cudaMemcpyDeviceToHost));
+        GSPH_CUDA(cudaMemcpy(ev.data(), s.ev[s.cur], n * 16, cudaMemcpyDeviceToHost));
+    }
+    const uint32_t S = uint32_t(s.scene_params.size());
+    std::vector<uint32_t> counts(S);
+    for (uint32_t k = 0; k < S; ++k) counts[k] = uint32_t(s.pbase[k + 1] - s.pbase[k]);
+    return snapshot_write(path, s.scene_params.data(), counts.data(), S, pos.data(),
+                          vel.data(), ev.data(), s.frames);
+}
+
+gsph_status gsph_snapshot_info(const char *path, uint32_t *n_scenes,
+                               uint64_t *n_particles, uint64_t *frames) {
+    return snapshot_header(path, n_scenes, n_particles, frames);
+}
+
+gsph_status gsph_snapshot_load(const char *path, int device, gsph_handle *out) {
+    if (!out) {
+        set_error("gsph_snapshot_load: null handle pointer");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    std::vector<gsph_params> plist;
+    std::vector<uint32_t> counts;
+    std::vector<float> pos, vel, ev;
+    uint64_t frames = 0;
+    gsph_status st = snapshot_read(path, plist, counts, pos, vel, ev, frames);
+    if (st) return st;
+    if (plist.empty()) {
+        set_error("snapshot %s holds no scene", path);
+        return GSPH_ERR_PARSE;
+    }
+    gsph_handle h = nullptr;
+    if (plist.size() == 1)
+        st = gsph_create(plist.data(), pos.data(), vel.data(), counts[0], device, &h);
+    else
+        st = gsph_batch_create(plist.data(), counts.data(), uint32_t(plist.size()),
+                               pos.data(), vel.data(), device, &h);
+    if (st) return st;
+    System &s = h->sys;
+    if (s.n > 0) {
+        cudaError_t e = cudaMemcpy(s.ev[s.cur], ev.data(), size_t(s.n) * 16,
+                                   cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            set_error("gsph_snapshot_load: %s", cudaGetErrorString(e));
+            gsph_destroy(h);
+            return GSPH_ERR_CUDA;
+        }
+    }
+    s.frames = frames;
+    *out = h;
+    return GSPH_OK;
+}
+
 gsph_status gsph_checksum(gsph_handle h, double out[5]) {
     gsph_status st = check_handle(h);
     if (st) return st;
@@ -1040,8 +1329,7 @@ gsph_status gsph_benchmark(gsph_handle h, int frames, gsph_bench_report *out) {
     const int measured = frames - warm;
     GSPH_CUDA(cudaStreamSynchronize(s.stream));
     const auto t0 = std::chrono::steady_clock::now();
-    for (int i = 0; i < measured; ++i)
-        if ((st = s.tick())) return st;
+    if ((st = s.step(measured))) return st;
     GSPH_CUDA(cudaStreamSynchronize(s.stream));
     const auto t1 = std::chrono::steady_clock::now();
     s.timing = old_timing;

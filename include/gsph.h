@@ -183,6 +183,21 @@ gsph_status gsph_create_from_json(const char *scene_path, int device,
                                   gsph_handle *out);
 gsph_status gsph_destroy(gsph_handle h);
 
+/* Snapshot / restart. gsph_snapshot_save writes every scene's parameters and
+ * particle count and the particle state (position with w = 1/rho, velocity,
+ * evaluated velocity with w = pressure) in the handle's current order, plus
+ * the frame counter, to a versioned binary file with a payload checksum.
+ * gsph_snapshot_load creates a handle (a batch when the file holds several
+ * scenes) that continues the run bit for bit: stepping it K frames gives the
+ * same state as stepping the saved handle K frames. gsph_snapshot_info reads
+ * the header only. Corrupted or foreign files fail with GSPH_ERR_PARSE. The
+ * reference has no restart path (its scenes always start from the JSON
+ * lattice, sph_hybrid_system.cpp:432-473). */
+gsph_status gsph_snapshot_save(gsph_handle h, const char *path);
+gsph_status gsph_snapshot_load(const char *path, int device, gsph_handle *out);
+gsph_status gsph_snapshot_info(const char *path, uint32_t *n_scenes,
+                               uint64_t *n_particles, uint64_t *frames);
+
 /* Batched step: num_scenes independent scenes stepped together, one launch
  * per stage for all of them (segmented grid sort over the concatenated cell
  * space, persistent density/force kernels over one work queue). params[k] is
@@ -195,6 +210,26 @@ gsph_status gsph_destroy(gsph_handle h);
 gsph_status gsph_batch_create(const gsph_params *params, const uint32_t *counts,
                               uint32_t num_scenes, const float *pos4,
                               const float *vel4, int device, gsph_handle *out);
+/* gsph_batch_create with room to grow: buffers sized for particle_capacity
+ * particles, cell_capacity cells and scene_capacity scenes (each at least
+ * the initial batch's), so gsph_batch_repack can change the scene set
+ * without reallocating. */
+gsph_status gsph_batch_create_ex(const gsph_params *params, const uint32_t *counts,
+                                 uint32_t num_scenes, const float *pos4,
+                                 const float *vel4, uint64_t particle_capacity,
+                                 uint64_t cell_capacity, uint32_t scene_capacity,
+                                 int device, gsph_handle *out);
+/* Changes the scene set between frames: the scenes listed in keep (current
+ * indices) stay, in that order, followed by n_add new scenes (parameters,
+ * counts, concatenated float4 positions / velocities; velocities may be
+ * NULL). Kept scenes continue exactly as if stepped alone. Fails with
+ * GSPH_ERR_CAPACITY, leaving the batch unchanged, when the new set does not
+ * fit the capacity. No counterpart in the reference (used by a serving loop
+ * that admits and retires scenes). */
+gsph_status gsph_batch_repack(gsph_handle h, const uint32_t *keep, uint32_t n_keep,
+                              const gsph_params *add_params, const uint32_t *add_counts,
+                              uint32_t n_add, const float *add_pos4,
+                              const float *add_vel4);
 /* Particle and cell offsets of the scenes: pbase_out[num_scenes + 1],
  * cbase_out[num_scenes + 1] (either may be NULL). Scene k's particles are
  * rows [pbase[k], pbase[k+1]) of every particle field. */
@@ -213,8 +248,11 @@ gsph_status gsph_arrange(gsph_handle h);
 gsph_status gsph_density(gsph_handle h);
 gsph_status gsph_force(gsph_handle h);
 gsph_status gsph_advance(gsph_handle h);
-/* Capture whole frames in CUDA graphs (1) or launch stage by stage (0). */
-gsph_status gsph_set_graph_mode(gsph_handle h, int enabled);
+/* frames > 0: gsph_step launches captured CUDA graphs of that many whole
+ * frames (any remainder frame by frame); 0: kernels are launched one by one.
+ * A frame needs no host synchronisation, so any number of frames can be
+ * captured. */
+gsph_status gsph_set_graph_mode(gsph_handle h, int frames);
 gsph_status gsph_sync(gsph_handle h);
 /* The handle's CUDA stream (a cudaStream_t), for callers that order their own
  * work or timing events against the handle's kernels. */

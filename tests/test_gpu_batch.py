@@ -86,3 +86,72 @@ def test_batch_handles_empty_scene(gsph, cuda_device):
     assert len(batched[1][0]) == 0
     assert _same(batched[0], _alone(gsph, p1, pos1, 5))
     assert _same(batched[2], _alone(gsph, p2, pos2, 5))
+
+
+def _load_serve(gsph):
+    import importlib.util
+    import sys
+    name = "gsph_gb300.serve"
+    if name not in sys.modules:
+        spec = importlib.util.spec_from_file_location(name, gsph.PKG_DIR / "serve.py")
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[name] = mod
+        spec.loader.exec_module(mod)
+    return sys.modules[name]
+
+
+def test_served_results_identical_alone_and_in_the_mix(gsph, cuda_device):
+    """Requests arrive while others are being stepped, are admitted between
+    chunks, share the batched step and retire at different frames; each
+    final state equals the scene stepped alone, bit for bit."""
+    serve = _load_serve(gsph)
+    specs = [(9, (0.5, 0.4, 0.4), 13, 0), (12, (0.7, 0.5, 0.5), 8, 3),
+             (7, (0.3, 0.3, 0.4), 17, 3), (14, (0.8, 0.5, 0.5), 6, 9),
+             (8, (0.4, 0.4, 0.4), 11, 14)]
+    reqs = []
+    for k, (n_side, box, steps, arrive) in enumerate(specs):
+        _, p, pos = dam_scene(gsph, n_side=n_side, box=box, seed=20 + k)
+        reqs.append((arrive, serve.Request(k, p, shuffled(pos, seed=k), steps, 0.0)))
+    alone = {}
+    for _, r in reqs:
+        with gsph.HybridSystem(params=r.params, positions=r.pos) as s:
+            s.step(r.steps)
+            alone[r.rid] = (s.copy_out(gsph.FIELD_POSITION), s.copy_out(gsph.FIELD_VELOCITY))
+    frame = [0]
+    srv = serve.SceneServer(gsph, budget_bytes=1 << 34, capacity=(200000, 400000, 16),
+                            chunk=4, clock=lambda: float(frame[0]))
+    pending = sorted(reqs, key=lambda x: x[0])
+    while pending or srv.queue or srv.resident:
+        while pending and pending[0][0] <= frame[0]:
+            srv.submit(pending.pop(0)[1])
+        srv.admit()
+        if srv.resident:
+            before = srv.frames
+            srv.step_chunk()
+            frame[0] += srv.frames - before
+        elif pending:
+            frame[0] = pending[0][0]
+    srv.close()
+    assert len(srv.done) == len(reqs)
+    for r in srv.done:
+        pos, vel = alone[r.rid]
+        assert np.array_equal(r.result["pos"].view(np.uint32), pos.view(np.uint32)), r.rid
+        assert np.array_equal(r.result["vel"].view(np.uint32), vel.view(np.uint32)), r.rid
+    # the mix really overlapped: some request waited for others and shared frames
+    assert any(r.t_admit > r.t_arrival for r in srv.done) or srv.frames < sum(
+        r.steps for r in srv.done)
+
+
+def test_repack_rejects_capacity_overflow(gsph, cuda_device):
+    _, p, pos = dam_scene(gsph, n_side=8)
+    with gsph.Batch([(p, pos)], capacity=(len(pos) + 10, p.numc * 2, 2)) as b:
+        with pytest.raises(gsph.GsphError) as ei:
+            b.repack([0], [(p, pos)])
+        assert ei.value.status == gsph.ERR_CAPACITY
+        b.step(2)                       # the batch is unchanged and usable
+        assert b.num_scenes == 1
+        b.repack([], [])                # no scene left: stepping is a no-op
+        b.step(3)
+        b.repack([], [(p, pos)])
+        b.step(1)
+        assert b.num_scenes == 1
