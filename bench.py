@@ -51,6 +51,47 @@ def dist_env():
     return ws, rank, local
 
 
+class Ranks:
+    """The replica group: one process per GPU under torchrun, joined over
+    torch.distributed (NCCL with GPUs, gloo without) for the barrier and the
+    max / sum over ranks; a no-op for a single process. Replicas exchange
+    nothing else: the path does not shard."""
+
+    def __init__(self, ws: int):
+        self.ws = ws
+        self.td = None
+        if ws > 1:
+            import torch
+            import torch.distributed as td
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if not td.is_initialized():
+                td.init_process_group(backend)
+            self.td = td
+            self.device = "cuda" if backend == "nccl" else "cpu"
+
+    def barrier(self):
+        if self.td:
+            self.td.barrier()
+
+    def _reduce(self, x: float, op) -> float:
+        if not self.td:
+            return float(x)
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64, device=self.device)
+        self.td.all_reduce(t, op=op)
+        return float(t.item())
+
+    def max(self, x: float) -> float:
+        return self._reduce(x, self.td.ReduceOp.MAX if self.td else None)
+
+    def sum(self, x: float) -> float:
+        return self._reduce(x, self.td.ReduceOp.SUM if self.td else None)
+
+    def close(self):
+        if self.td and self.td.is_initialized():
+            self.td.destroy_process_group()
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -153,24 +194,19 @@ def load_pkg():
     return ge.package()
 
 
-def cpu_oracle_rate(g, budget_s: float, max_steps: int, sample_n: int | None = None):
-    """FP64 oracle frames on the scene (optionally its first sample_n
-    particles); returns (particle-steps/s, steps, particles, threads)."""
+def cpu_oracle_rate(params, pos, budget_s: float, max_steps: int, vel=None, ev=None):
+    """FP64 oracle frames on the given state (all host threads); returns
+    (particle-steps/s, steps, particles, threads)."""
     import oracle
     oracle.build()
-    s = g.load_scene(g.scene_path(SCENE))
-    p = g.params_init(s)
-    pos = g.lattice(s, p)
-    if sample_n is not None and sample_n < len(pos):
-        pos = pos[:sample_n].copy()
-    vel = np.zeros_like(pos)
-    ev = np.zeros_like(pos)
-    P, V, E = (np.array(a, np.float64) for a in (pos, vel, ev))
+    P = np.array(pos, np.float64)
+    V = np.zeros_like(P) if vel is None else np.array(vel, np.float64)
+    E = np.zeros_like(P) if ev is None else np.array(ev, np.float64)
     lib = oracle._load()
     steps = 0
     t0 = time.perf_counter()
     while steps < max_steps:
-        lib.oracle_step(P.ctypes.data, V.ctypes.data, E.ctypes.data, len(P), oracle._ref(p))
+        lib.oracle_step(P.ctypes.data, V.ctypes.data, E.ctypes.data, len(P), oracle._ref(params))
         steps += 1
         if time.perf_counter() - t0 >= budget_s:
             break
@@ -243,6 +279,7 @@ def run_batched(args, ws, rank, local):
     scenes with the plain single-scene path."""
     import torch
     torch.cuda.set_device(local)
+    R = Ranks(ws)
     g = load_pkg()
     W = load_workloads()
     specs = W.batched_scenes(args.scenes, seed=rank)
@@ -257,6 +294,7 @@ def run_batched(args, ws, rank, local):
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     clocks = ClockSampler(local)
+    R.barrier()
     torch.cuda.synchronize()
     clocks.start()
     time.sleep(0.3)
@@ -270,7 +308,9 @@ def run_batched(args, ws, rank, local):
     dev_ms = ev0.elapsed_time(ev1)
     info = b.info()
     b.close()
-    batched = total * K / (dev_ms / 1e3)
+    dev_ms = R.max(dev_ms)
+    total_all = R.sum(total)
+    batched = total_all * K / (dev_ms / 1e3)
 
     def loop_rate(graph_frames):
         hs = [g.HybridSystem(params=p, positions=pos, device=local) for p, pos in scenes]
@@ -278,15 +318,16 @@ def run_batched(args, ws, rank, local):
             h.set_graph_mode(graph_frames)
             h.step(args.warmup)
             h.sync()
+        R.barrier()
         torch.cuda.synchronize()
         t = time.perf_counter()
         for h in hs:
             h.step(K)
             h.sync()
-        dt = time.perf_counter() - t
+        dt = R.max(time.perf_counter() - t)
         for h in hs:
             h.close()
-        return total * K / dt, dt
+        return total_all * K / dt, dt
 
     loop_plain, t_plain = loop_rate(0)
     loop_graph, t_graph = loop_rate(args.graph_frames)
@@ -296,7 +337,7 @@ def run_batched(args, ws, rank, local):
         "warmup": args.warmup, "ms_per_step": dev_ms / K, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: seeded jittered dam-break columns generated on the host",
-        "config": {"workload": f"batched: {len(scenes)} scenes, {total} particles, "
+        "config": {"workload": f"batched: {len(scenes)} scenes per GPU, {total} particles, "
                                f"N log-uniform [4096, 262144], aspect U[0.5, 2], "
                                f"262k-scene physics, own boxes",
                    "graph_frames": args.graph_frames, "cells": int(info.n_cells)},
@@ -313,6 +354,7 @@ def run_batched(args, ws, rank, local):
     }
     if rank == 0:
         print(json.dumps(line))
+    R.close()
     return 0
 
 
@@ -381,6 +423,7 @@ def run_served(args, ws, rank, local):
     and retires each after its K frames (its positions are read back)."""
     import torch
     torch.cuda.set_device(local)
+    R = Ranks(ws)
     g = load_pkg()
     W = load_workloads()
     S = load_serve()
@@ -397,6 +440,7 @@ def run_served(args, ws, rank, local):
         h.sync()
 
     done_submitting = threading.Event()
+    R.barrier()
     t0 = time.perf_counter()
     errors = []
 
@@ -450,7 +494,8 @@ def run_served(args, ws, rank, local):
     srv.close()
     if errors:
         raise errors[0]
-    served = srv.particle_steps / makespan
+    makespan = R.max(makespan)
+    served = R.sum(srv.particle_steps) / makespan
     lat = S.latency_stats(srv.done)
     offered = sum(sp["nx"] * sp["ny"] * sp["nz"] * k for _, sp, k in trace)
     loop = fifo_loop_model(g, W, trace, local, args.warmup)
@@ -480,6 +525,7 @@ def run_served(args, ws, rank, local):
     }
     if rank == 0:
         print(json.dumps(line))
+    R.close()
     return 0
 
 
@@ -493,7 +539,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true",
                     help="skip the end-to-end loop (profiling runs)")
     ap.add_argument("--scene", default=SCENE)
-    ap.add_argument("--workload", default="single", choices=["single", "batched", "served"])
+    ap.add_argument("--workload", default="single", choices=["single", "batched", "served", "stress"])
     ap.add_argument("--scenes", type=int, default=256, help="batched: scene count")
     ap.add_argument("--graph-frames", type=int, default=10)
     ap.add_argument("--duration", type=float, default=60.0, help="served: seconds of traffic")
@@ -501,6 +547,9 @@ def main():
     ap.add_argument("--cap-particles", type=int, default=40_000_000,
                     help="served: particle capacity of the resident batch")
     ap.add_argument("--chunk", type=int, default=10, help="served: frames between admissions")
+    ap.add_argument("--stress-side", type=int, default=256, help="stress: column side")
+    ap.add_argument("--restart-frames", type=int, default=2000,
+                    help="stress: frames before the snapshot")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":
@@ -511,14 +560,69 @@ def main():
         return run_served(args, ws, rank, local)
 
     import torch
-    dist = None
-    if ws > 1:
-        import torch.distributed as tdist
-        tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-        dist = tdist
     torch.cuda.set_device(local)
+    dist = Ranks(ws)
     g = load_pkg()
-    sysm = g.HybridSystem(g.scene_path(args.scene), device=local)
+    if args.workload == "stress":
+        sysm, workload, cpu_state = prepare_stress(g, args, local)
+    else:
+        sysm = g.HybridSystem(g.scene_path(args.scene), device=local)
+        workload = WORKLOAD if args.scene == SCENE else args.scene
+        s = g.load_scene(g.scene_path(args.scene))
+        p = g.params_init(s)
+        cpu_state = (p, g.lattice(s, p), None, None,
+                     "FP64 frame(s) of the full {n}-particle scene")
+    line = measure_scene(g, sysm, args, ws, rank, local, dist, workload, cpu_state)
+    if line is not None:
+        print(json.dumps(line))
+    dist.close()
+    return 0
+
+
+def prepare_stress(g, args, local):
+    """256^3 = 16,777,216-particle column with the 262,144-particle scene's
+    physics and proportions (box 10.24 x 5.12 x 5.12 m, 512 x 256 x 256
+    cells), stepped `restart_frames` frames from the lattice with CUDA graphs,
+    saved to a snapshot and restarted from it."""
+    import tempfile
+    W = load_workloads()
+    side = args.stress_side
+    s = g.parse_scene(W.column_scene_text(side, side, side, seed=0))
+    p = g.params_init(s)
+    pos = g.lattice(s, p)
+    t = time.perf_counter()
+    with g.HybridSystem(params=p, positions=pos, device=local) as h:
+        h.set_graph_mode(50)
+        h.step(args.restart_frames)
+        h.sync()
+        gen_s = time.perf_counter() - t
+        fd, path = tempfile.mkstemp(suffix=".gsnap")
+        os.close(fd)
+        h.save_snapshot(path)
+    del pos
+    try:
+        sysm = g.load_snapshot(path, device=local)
+    finally:
+        os.remove(path)
+    sysm.arrange()                 # the grid of the restarted state
+    cnt = sysm.copy_out(g.FIELD_CELL_COUNT)
+    occ = cnt[cnt > 0]
+    workload = (f"stress: {side}^3 = {side ** 3:,} FP32 particles restarted from a snapshot "
+                f"after {args.restart_frames} frames of the 262k dam-break physics "
+                f"(generated in {gen_s:.1f} s); grid {tuple(p.grid_size)}, occupied cells "
+                f"{len(occ):,}, occupancy mean {occ.mean():.2f}, max {int(occ.max())} "
+                f"({occ.max() / occ.mean():.2f}x mean)")
+    sample = min(2_000_000, sysm.n)
+    spos = sysm.copy_out(g.FIELD_POSITION)[:sample].copy()
+    svel = sysm.copy_out(g.FIELD_VELOCITY)[:sample].copy()
+    sev = sysm.copy_out(g.FIELD_EVAL_VELOCITY)[:sample].copy()
+    return sysm, workload, (p, spos, svel, sev,
+                            "FP64 frame(s) of the first {n} particles (sorted order) of the "
+                            "restarted state")
+
+
+def measure_scene(g, sysm, args, ws, rank, local, dist, workload, cpu_state):
+    import torch
     n = sysm.n
     stream = torch.cuda.ExternalStream(sysm.stream(), device=torch.device("cuda", local))
 
@@ -532,8 +636,7 @@ def main():
     clocks = ClockSampler(local)
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
-    if dist:
-        dist.barrier()
+    dist.barrier()
     torch.cuda.synchronize()
     clocks.start()
     time.sleep(0.3)
@@ -546,10 +649,7 @@ def main():
     elapsed_ms = ev0.elapsed_time(ev1)
     stages = sysm.stage_times()
     sysm.set_stage_timing(False)
-    if dist:
-        t = torch.tensor([elapsed_ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
+    elapsed_ms = dist.max(elapsed_ms)
     sysm.sync()
     ms_per_step = elapsed_ms / max(args.steps, 1)
     value = ws * n * args.steps / (elapsed_ms / 1e3)
@@ -566,6 +666,14 @@ def main():
     # the stage is one TRA and one SMS launch; name the one that does the work
     kernel = f"k_{dom}_" + ("sms" if info.tra_particles == 0 else "tra")
     traffic = ncu_traffic(kernel)
+    # both passes against the same cell-tile model (each stage = its TRA and
+    # SMS launches back to back)
+    per_stage = {}
+    for st, b in (("density", b_den), ("force", b_for)):
+        t_s = stages[st] / 1e3
+        a = b / t_s / 1e9 if t_s > 0 else 0.0
+        per_stage[st] = {"achieved": a, "frac": a / peak, "algorithmic_bytes": b,
+                         "ms": stages[st]}
 
     # end to end through the public API: host-resident state, pinned buffers
     host = [torch.empty((n, 4), dtype=torch.float32, pin_memory=True) for _ in range(3)]
@@ -574,8 +682,7 @@ def main():
         sysm.copy_out_async(f, h.data_ptr(), h.numel() * 4)
     sysm.sync()
     e2e_steps = 0 if args.no_e2e else max(3, min(args.steps, 20))
-    if dist:
-        dist.barrier()
+    dist.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
@@ -586,30 +693,29 @@ def main():
             sysm.copy_out_async(f, h.data_ptr(), h.numel() * 4)
         sysm.sync()
     e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = dist.max(e2e_s)
     e2e_value = ws * n * e2e_steps / e2e_s if e2e_steps else None
     state_bytes = 3 * n * 16
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        rate, steps, cnt, thr = cpu_oracle_rate(g, budget_s=12.0, max_steps=4)
+        cp, cpos, cvel, cev, what = cpu_state
+        rate, steps, cnt, thr = cpu_oracle_rate(cp, cpos, budget_s=12.0, max_steps=4,
+                                                vel=cvel, ev=cev)
         cpu = {"value": rate, "unit": "particle-steps/s", "cores": thr, "kind": "port",
-               "sample": f"{steps} FP64 frame(s) of the full {cnt}-particle scene "
-                         f"(C/OpenMP restatement of the reference step)"}
+               "sample": f"{steps} " + what.format(n=cnt) +
+                         " (C/OpenMP restatement of the reference step)"}
     sysm.close()
     if rank != 0:
-        return 0
+        return None
     line = {
         "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: seeded jittered dam-break lattice generated on the host",
-        "config": {"workload": WORKLOAD, "particles": n,
+        "config": {"workload": workload, "particles": n,
                    "parallelism": f"{ws} independent replica(s)" if ws > 1 else "single GPU",
-                   "l2": "no flush: 440 MB particle state per frame > 129 MB L2",
+                   "l2": f"no flush: {n * 112 / 1e6:.0f} MB particle state per frame > 129 MB L2",
                    "timing": "CUDA events on the scene stream, stage events inside"},
         "stages_ms": stages,
         "split": {"tra_particles": info.tra_particles, "sms_tasks": info.sms_tasks,
@@ -619,6 +725,7 @@ def main():
                      "traffic": traffic, "algorithmic_bytes": b_dom,
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
                      if peak_kind == "measured" else "fallback 6800 GB/s"},
+        "roofline_stages": per_stage,
         "e2e": {"value": e2e_value, "unit": "particle-steps/s",
                 "h2d_bytes_per_step": state_bytes, "d2h_bytes_per_step": state_bytes,
                 "steps": e2e_steps},
@@ -626,10 +733,9 @@ def main():
         "clocks": clk,
         "gpu_launches": LAUNCHES_PER_FRAME * args.steps,
     }
-    print(json.dumps(line))
-    if dist:
-        dist.destroy_process_group()
-    return 0
+    return line
+
+
 
 
 if __name__ == "__main__":

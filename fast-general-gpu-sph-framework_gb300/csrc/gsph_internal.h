@@ -126,6 +126,10 @@ struct Frame {
     SceneTable scenes;
     const float4 *pos_in, *vel_in, *ev_in;     // unsorted (previous order)
     float4 *pos, *vel, *ev, *acc;              // sorted (current order)
+    // Sorted positions as separate x / y / z arrays (written by the sort,
+    // read by the TRA density pass two candidates at a time); null when the
+    // caller does not keep them. Two padding slots follow the last particle.
+    float *sx, *sy, *sz;
     uint32_t *key_in, *slot;                   // per source particle
     unsigned long long *pairs;                 // (key << 32 | src), by cell
     uint32_t *key;                             // sorted keys

@@ -97,6 +97,7 @@ struct System {
     Frame fr{};    // pointers shared by both parities
     double *red = nullptr;   // reductions workspace
     bool arranged = false;   // sorted state + split valid
+    bool grid_current = false;   // no position changed since the last arrange
     bool lists_valid = false;   // TRA neighbour masks match the state
     uint64_t frames = 0;
 
@@ -273,7 +274,9 @@ struct System {
                 (st = alloc_n(&ev[b], N)))
                 return st;
         }
-        if ((st = alloc_n(&acc, N)) || (st = alloc_n(&fr.key_in, N)) ||
+        if ((st = alloc_n(&acc, N)) || (st = alloc_n(&fr.sx, N + 2)) ||
+            (st = alloc_n(&fr.sy, N + 2)) || (st = alloc_n(&fr.sz, N + 2)) ||
+            (st = alloc_n(&fr.key_in, N)) ||
             (st = alloc_n(&fr.slot, N)) || (st = alloc_n(&fr.pairs, N)) ||
             (st = alloc_n(&fr.key, N)) || (st = alloc_n(&fr.perm, N)) ||
             (st = alloc_n(&fr.cell_count, C)) ||
@@ -309,6 +312,8 @@ struct System {
             GSPH_CUDA(cudaMemsetAsync(ev[b], 0, sizeof(float4) * N, stream));
         }
         GSPH_CUDA(cudaMemsetAsync(acc, 0, sizeof(float4) * N, stream));
+        for (float *a : {fr.sx, fr.sy, fr.sz})
+            GSPH_CUDA(cudaMemsetAsync(a, 0, sizeof(float) * (N + 2), stream));
         if (n > 0) {
             GSPH_CUDA(cudaMemcpyAsync(pos[0], pos4, sizeof(float4) * n,
                                       cudaMemcpyHostToDevice, stream));
@@ -413,6 +418,7 @@ struct System {
         set_counts(int(n_total), int(c_total));
         if ((st = upload_table())) return st;
         arranged = false;
+        grid_current = false;
         lists_valid = false;
         GSPH_CUDA(cudaStreamSynchronize(stream));
         return GSPH_OK;
@@ -542,6 +548,7 @@ struct System {
         if (st) return st;
         cur = out;
         arranged = true;
+        grid_current = false;
         ++frames;
         return GSPH_OK;
     }
@@ -558,6 +565,7 @@ struct System {
                 GSPH_CUDA(cudaGraphLaunch(graph[cur], stream));
                 if (graph_frames & 1) cur = 1 - cur;
                 arranged = true;
+                grid_current = false;
                 lists_valid = false;
                 frames += uint64_t(graph_frames);
                 n -= graph_frames;
@@ -892,12 +900,13 @@ gsph_status gsph_arrange(gsph_handle h) {
     if ((st = s.check_launch())) return st;
     s.cur = 1 - s.cur;
     s.arranged = true;
+    s.grid_current = true;
     return GSPH_OK;
 }
 
 static gsph_status need_arranged(System &s) {
-    if (!s.arranged) {
-        set_error("the grid has not been arranged yet (call gsph_arrange)");
+    if (!s.arranged || !s.grid_current) {
+        set_error("positions changed since the last arrange (call gsph_arrange)");
         return GSPH_ERR_STATE;
     }
     return GSPH_OK;
@@ -921,6 +930,7 @@ gsph_status gsph_advance(gsph_handle h) {
     gsph_status st = check_handle(h);
     if (st) return st;
     h->sys.enqueue_advance(h->sys.cur);
+    h->sys.grid_current = false;
     return h->sys.check_launch();
 }
 
@@ -1164,6 +1174,8 @@ gsph_status gsph_copy_in(gsph_handle h, gsph_field field, const void *host_src,
     GSPH_CUDA(cudaStreamSynchronize(s.stream));
     if (bytes) GSPH_CUDA(cudaMemcpy(dst, host_src, bytes, cudaMemcpyHostToDevice));
     s.lists_valid = false;   // the masks describe the old state
+    // new positions need a new grid (cell lists and the sorted x/y/z copy)
+    if (field == GSPH_FIELD_POSITION) s.grid_current = false;
     return GSPH_OK;
 }
 
@@ -1181,6 +1193,7 @@ gsph_status gsph_copy_in_async(gsph_handle h, gsph_field field,
         GSPH_CUDA(cudaMemcpyAsync(dst, host_src, bytes, cudaMemcpyHostToDevice,
                                   s.stream));
     s.lists_valid = false;   // the masks describe the old state
+    if (field == GSPH_FIELD_POSITION) s.grid_current = false;
     return GSPH_OK;
 }
 

@@ -242,7 +242,10 @@ gsph_status gsph_batch_ranges(gsph_handle h, int32_t *pbase_out,
 gsph_status gsph_copy_out_scene(gsph_handle h, uint32_t scene, gsph_field field,
                                 void *host_dst, size_t bytes);
 
-/* One frame = arrange + density + force + advance (tick). */
+/* One frame = arrange + density + force + advance (tick). gsph_density and
+ * gsph_force need the grid of the current positions: they fail with
+ * GSPH_ERR_STATE after gsph_advance, a frame, or a position copy-in until
+ * gsph_arrange has run again. */
 gsph_status gsph_step(gsph_handle h, int n_steps);
 gsph_status gsph_arrange(gsph_handle h);
 gsph_status gsph_density(gsph_handle h);
