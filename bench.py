@@ -287,8 +287,14 @@ def run_batched(args, ws, rank, local):
     total = sum(len(pos) for _, pos in scenes)
     K = args.steps
     b = g.Batch(scenes, device=local)
-    b.set_graph_mode(args.graph_frames)
     b.step(args.warmup)
+    b.sync()
+    tuned = None
+    if not args.no_autotune:
+        t, ms = b.autotune(frames_per_trial=3)
+        tuned = {**t.as_dict(), "trial_ms_per_frame": ms}
+    b.set_graph_mode(args.graph_frames)
+    b.step(1)
     b.sync()
     stream = torch.cuda.ExternalStream(b.stream(), device=torch.device("cuda", local))
     ev0 = torch.cuda.Event(enable_timing=True)
@@ -340,7 +346,8 @@ def run_batched(args, ws, rank, local):
         "config": {"workload": f"batched: {len(scenes)} scenes per GPU, {total} particles, "
                                f"N log-uniform [4096, 262144], aspect U[0.5, 2], "
                                f"262k-scene physics, own boxes",
-                   "graph_frames": args.graph_frames, "cells": int(info.n_cells)},
+                   "graph_frames": args.graph_frames, "cells": int(info.n_cells),
+                   "tuning": tuned if tuned else "reference thresholds, default shapes"},
         "batched_wall_s": wall_b,
         "per_scene_loop": {"value": loop_plain, "unit": "particle-steps/s",
                            "wall_s": t_plain, "launch": "kernel by kernel"},
@@ -542,6 +549,8 @@ def main():
     ap.add_argument("--workload", default="single", choices=["single", "batched", "served", "stress"])
     ap.add_argument("--scenes", type=int, default=256, help="batched: scene count")
     ap.add_argument("--graph-frames", type=int, default=10)
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="batched: keep the reference thresholds and default shapes")
     ap.add_argument("--duration", type=float, default=60.0, help="served: seconds of traffic")
     ap.add_argument("--budget-gb", type=float, default=150.0, help="served: HBM state budget")
     ap.add_argument("--cap-particles", type=int, default=40_000_000,

@@ -137,6 +137,17 @@ class Info(C.Structure):
     ]
 
 
+class Tuning(C.Structure):
+    """gsph_tuning: split thresholds and CTAs per SM of the density/force
+    kernels (defaults: the reference's 96 / 15 / 60 and 6 / 6 / 4 / 4)."""
+    _fields_ = [(n, C.c_int32) for n in (
+        "sparse_total", "sparse_self", "mid_total", "ctas_density_tra",
+        "ctas_density_sms", "ctas_force_tra", "ctas_force_sms", "reserved_")]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved_"}
+
+
 class BenchReport(C.Structure):
     _fields_ = [
         ("measured_frames", C.c_int32), ("warmup_frames", C.c_int32),
@@ -195,6 +206,11 @@ _SIGS = {
     "gsph_copy_in_async": ([_VP, C.c_int, _VP, C.c_size_t], C.c_int),
     "gsph_copy_out_async": ([_VP, C.c_int, _VP, C.c_size_t], C.c_int),
     "gsph_checksum": ([_VP, C.POINTER(C.c_double)], C.c_int),
+    "gsph_tuning_default": ([C.POINTER(Tuning)], C.c_int),
+    "gsph_get_tuning": ([_VP, C.POINTER(Tuning)], C.c_int),
+    "gsph_set_tuning": ([_VP, C.POINTER(Tuning)], C.c_int),
+    "gsph_autotune": ([_VP, C.c_int, C.POINTER(Tuning), C.c_int, C.POINTER(Tuning),
+                       C.POINTER(C.c_float)], C.c_int),
     "gsph_reductions": ([_VP, C.POINTER(C.c_double)], C.c_int),
     "gsph_benchmark": ([_VP, C.c_int, C.POINTER(BenchReport)], C.c_int),
     "gsph_set_stage_timing": ([_VP, C.c_int], C.c_int),
@@ -431,6 +447,27 @@ class HybridSystem:
         keys = ("mass", "px", "py", "pz", "kinetic", "sx", "sy", "sz")
         return dict(zip(keys, out))
 
+    def get_tuning(self) -> Tuning:
+        t = Tuning()
+        _check(self._lib.gsph_get_tuning(self._h, C.byref(t)))
+        return t
+
+    def set_tuning(self, t: Tuning) -> None:
+        _check(self._lib.gsph_set_tuning(self._h, C.byref(t)))
+
+    def autotune(self, frames_per_trial: int = 3, candidates=None):
+        """gsph_autotune: times the candidates (None: the built-in grid) on the
+        current state, installs the fastest; returns (Tuning, ms per frame)."""
+        best, ms = Tuning(), C.c_float()
+        if candidates is None:
+            arr, n = None, 0
+        else:
+            arr = (Tuning * len(candidates))(*candidates)
+            n = len(candidates)
+        _check(self._lib.gsph_autotune(self._h, frames_per_trial, arr, n, C.byref(best),
+                                       C.byref(ms)))
+        return best, ms.value
+
     def save_snapshot(self, path: os.PathLike | str) -> None:
         """gsph_snapshot_save: the state, parameters and frame counter."""
         _check(self._lib.gsph_snapshot_save(self._h, str(path).encode()))
@@ -445,6 +482,50 @@ class HybridSystem:
     @property
     def handle(self) -> int:
         return self._h.value
+
+
+def tuning_default() -> Tuning:
+    t = Tuning()
+    _check(load_library().gsph_tuning_default(C.byref(t)))
+    return t
+
+
+def occupancy_signature(cell_count: np.ndarray, n_particles: int) -> tuple:
+    """Occupancy histogram of the occupied cells in power-of-two bins (1,
+    2-3, 4-7, ..., >= 512), as fractions rounded to 0.05, with the particle
+    count's power of two: the key under which Autotuner caches a tuning."""
+    occ = np.asarray(cell_count)[np.asarray(cell_count) > 0]
+    if occ.size == 0:
+        return (0,)
+    b = np.minimum(np.floor(np.log2(occ)).astype(np.int64), 9)
+    h = np.bincount(b, minlength=10) / occ.size
+    return (int(np.log2(max(n_particles, 1))),) + tuple(float(round(x * 20) / 20) for x in h)
+
+
+class Autotuner:
+    """Tunings per occupancy histogram: the first handle with a new signature
+    is autotuned (gsph_autotune), later ones with the same signature get the
+    cached result without any trial frames."""
+
+    def __init__(self, frames_per_trial: int = 3, candidates=None):
+        self.frames = frames_per_trial
+        self.candidates = candidates
+        self.cache: dict[tuple, tuple[Tuning, float]] = {}
+
+    def signature(self, h: "HybridSystem") -> tuple:
+        h.arrange()
+        return occupancy_signature(h.copy_out(FIELD_CELL_COUNT), h.n)
+
+    def tune(self, h: "HybridSystem") -> tuple[Tuning, float, bool]:
+        """Returns (tuning, ms per frame at tuning time, came from the cache)."""
+        sig = self.signature(h)
+        if sig in self.cache:
+            t, ms = self.cache[sig]
+            h.set_tuning(t)
+            return t, ms, True
+        t, ms = h.autotune(self.frames, self.candidates)
+        self.cache[sig] = (t, ms)
+        return t, ms, False
 
 
 def snapshot_info(path: os.PathLike | str) -> dict:

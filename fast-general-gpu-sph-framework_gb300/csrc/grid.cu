@@ -250,13 +250,7 @@ __device__ __forceinline__ void move_particle(const Frame &f, int dst,
     const int src = int(e & 0xFFFFFFFFull);
     f.key[dst] = uint32_t(e >> 32);
     f.perm[dst] = src;
-    const float4 q = f.pos_in[src];
-    f.pos[dst] = q;
-    if (f.sx) {
-        f.sx[dst] = q.x;
-        f.sy[dst] = q.y;
-        f.sz[dst] = q.z;
-    }
+    f.pos[dst] = f.pos_in[src];
     f.vel[dst] = f.vel_in[src];
     f.ev[dst] = f.ev_in[src];
 }

@@ -57,6 +57,7 @@ struct DevParams {
     float time_step, wall_damping, wall_kernel;   // wall_kernel = h + 0.01
     float gx_acc, gy_acc, gz_acc;                 // gravity
     float bmin;                                   // lower wall (= h) on every axis
+    int sparse_total, sparse_self, mid_total;     // split thresholds (gsph_tuning)
 };
 
 // Geometry of one scene of a batch. Particles of scene s occupy
@@ -126,10 +127,6 @@ struct Frame {
     SceneTable scenes;
     const float4 *pos_in, *vel_in, *ev_in;     // unsorted (previous order)
     float4 *pos, *vel, *ev, *acc;              // sorted (current order)
-    // Sorted positions as separate x / y / z arrays (written by the sort,
-    // read by the TRA density pass two candidates at a time); null when the
-    // caller does not keep them. Two padding slots follow the last particle.
-    float *sx, *sy, *sz;
     uint32_t *key_in, *slot;                   // per source particle
     unsigned long long *pairs;                 // (key << 32 | src), by cell
     uint32_t *key;                             // sorted keys
@@ -162,12 +159,18 @@ void launch_cell_sort(const Frame &f, int num_sms, cudaStream_t s);
 void launch_split(const Frame &f, const DevParams &P, int max_occ,
                   cudaStream_t s);
 // ---- launchers (physics.cu) ----
+// Launch shapes of the density and force passes: CTAs per SM of each kernel.
+struct LaunchShape {
+    int density_tra, density_sms, force_tra, force_sms;
+};
+constexpr LaunchShape kMaxShape = {6, 6, 4, 4};   // the kernels' launch bounds
+
 void launch_density(const Frame &f, const DevParams &P, int num_sms,
-                    cudaStream_t s);
+                    const LaunchShape &shape, cudaStream_t s);
 // fresh: the density pass ran on the current state, so the TRA neighbour
 // masks are valid.
 void launch_force(const Frame &f, const DevParams &P, int num_sms, bool fresh,
-                  cudaStream_t s);
+                  const LaunchShape &shape, cudaStream_t s);
 void launch_integrate(const Frame &f, const DevParams &P, cudaStream_t s);
 void launch_reductions(const float4 *pos, const float4 *vel, int n,
                        float mass, double *out8, cudaStream_t s);

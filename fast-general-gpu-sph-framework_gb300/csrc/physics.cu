@@ -209,32 +209,13 @@ __device__ __forceinline__ int next_unit(int *counter) {
 
 // ------------------------------------------------------------ density TRA --
 // One particle per lane, 32 consecutive TRA particles per work unit
-// (density_kernels.cu:318-366). Candidates are read from the sorted x/y/z
-// arrays two at a time and evaluated with packed FP32x2 arithmetic (an odd
-// first or last candidate of a row alone, with the same scalar roundings).
-// Which candidates of each row interact is also recorded as a bit mask for
-// the force pass.
-// One candidate j alone: adds (h^2 - r^2)^3 to sum, returns whether it
-// interacts. Every term is rounded as in the paired loop below and added in
-// candidate order, so the sum does not depend on where the pairs start (a
-// scene's rows start at different parities alone and inside a batch).
-__device__ __forceinline__ bool density_one(const Frame &f, int j, float4 p,
-                                            float h2, float &sum) {
-    const float d2 = sq_dist(f.sx[j] - p.x, f.sy[j] - p.y, f.sz[j] - p.z);
-    float t = __fmaf_rn(d2, -1.f, h2);
-    const bool in = !(t < 0.f || d2 < kFloatSmall);
-    t = in ? t : 0.f;
-    sum = __fadd_rn(sum, __fmul_rn(__fmul_rn(t, t), t));
-    return in;
-}
-
+// (density_kernels.cu:318-366). Which candidates of each row interact is also
+// recorded as a bit mask for the force pass.
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, 6)
 k_density_tra(Frame f, DevParams P) {
     const int lane = threadIdx.x & 31;
     const int middle = f.ctr->middle;
     const int units = (middle + 31) >> 5;
-    const float2 h2v = make_float2(P.h2, P.h2);
-    const float2 m1 = make_float2(-1.f, -1.f);
     for (;;) {
         const int u = next_unit(&f.ctr->work_density);
         if (u >= units) break;
@@ -244,9 +225,6 @@ k_density_tra(Frame f, DevParams P) {
         const float4 p = f.pos[self];
         const SceneGeom G = geom_of_particle(f.scenes, self);
         const MicroPos mp = micro_of(p, P, G);
-        const float2 npx = make_float2(-p.x, -p.x);
-        const float2 npy = make_float2(-p.y, -p.y);
-        const float2 npz = make_float2(-p.z, -p.z);
         uint32_t *masks = f.nbr_mask + size_t(u) * 9 * 32 + lane;
         int incomplete = 0;
         int found = 0;
@@ -260,34 +238,17 @@ k_density_tra(Frame f, DevParams P) {
                 int begin, end;
                 row_range(f, G, m, mp.cx, mp.lmx, mp.lmx, begin, end);
                 incomplete |= (end - begin > kMaskRowMax);
-                int j = begin;
                 uint32_t bit = 1u;
-                if ((j & 1) && j < end) {
-                    if (density_one(f, j, p, P.h2, sum)) mask |= bit;
-                    ++j;
-                    bit <<= 1;
+#pragma unroll 8
+                for (int j = begin; j < end; ++j, bit <<= 1) {
+                    const float4 q = f.pos[j];
+                    const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+                    const float d2 = sq_dist(dx, dy, dz);
+                    if (P.h2 < d2 || kFloatSmall > d2) continue;
+                    const float t = P.h2 - d2;
+                    sum += t * t * t;
+                    mask |= bit;
                 }
-#pragma unroll 2
-                for (; j + 1 < end; j += 2, bit <<= 2) {
-                    const float2 X = *reinterpret_cast<const float2 *>(f.sx + j);
-                    const float2 Y = *reinterpret_cast<const float2 *>(f.sy + j);
-                    const float2 Z = *reinterpret_cast<const float2 *>(f.sz + j);
-                    const float2 dx = __fadd2_rn(X, npx);
-                    const float2 dy = __fadd2_rn(Y, npy);
-                    const float2 dz = __fadd2_rn(Z, npz);
-                    float2 d2 = __fmul2_rn(dx, dx);
-                    d2 = __ffma2_rn(dy, dy, d2);
-                    d2 = __ffma2_rn(dz, dz, d2);
-                    float2 t = __ffma2_rn(d2, m1, h2v);
-                    const bool in0 = !(t.x < 0.f || d2.x < kFloatSmall);
-                    const bool in1 = !(t.y < 0.f || d2.y < kFloatSmall);
-                    t.x = in0 ? t.x : 0.f;
-                    t.y = in1 ? t.y : 0.f;
-                    const float2 t3 = __fmul2_rn(__fmul2_rn(t, t), t);
-                    sum = __fadd_rn(__fadd_rn(sum, t3.x), t3.y);
-                    mask |= (in0 ? bit : 0u) | (in1 ? (bit << 1) : 0u);
-                }
-                if (j < end && density_one(f, j, p, P.h2, sum)) mask |= bit;
             }
             masks[r * 32] = mask;
             found += __popc(mask);
@@ -740,17 +701,17 @@ k_final_sum(const double *__restrict__ part, int nparts, double *__restrict__ ou
 }  // namespace
 
 void launch_density(const Frame &f, const DevParams &P, int num_sms,
-                    cudaStream_t s) {
+                    const LaunchShape &shape, cudaStream_t s) {
     if (f.n <= 0) return;
-    k_density_tra<<<num_sms * 6, kWarpsPerBlock * 32, 0, s>>>(f, P);
-    k_density_sms<<<num_sms * 6, kWarpsPerBlock * 32, 0, s>>>(f, P);
+    k_density_tra<<<num_sms * shape.density_tra, kWarpsPerBlock * 32, 0, s>>>(f, P);
+    k_density_sms<<<num_sms * shape.density_sms, kWarpsPerBlock * 32, 0, s>>>(f, P);
 }
 
 void launch_force(const Frame &f, const DevParams &P, int num_sms, bool fresh,
-                  cudaStream_t s) {
+                  const LaunchShape &shape, cudaStream_t s) {
     if (f.n <= 0) return;
-    k_force_tra<<<num_sms * 4, kWarpsPerBlock * 32, 0, s>>>(f, P, fresh);
-    k_force_sms<<<num_sms * 4, kWarpsPerBlock * 32, 0, s>>>(f, P);
+    k_force_tra<<<num_sms * shape.force_tra, kWarpsPerBlock * 32, 0, s>>>(f, P, fresh);
+    k_force_sms<<<num_sms * shape.force_sms, kWarpsPerBlock * 32, 0, s>>>(f, P);
 }
 
 void launch_integrate(const Frame &f, const DevParams &P, cudaStream_t s) {

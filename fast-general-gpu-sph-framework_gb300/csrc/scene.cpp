@@ -234,6 +234,9 @@ DevParams make_dev_params(const gsph_params &p) {
     d.gy_acc = p.gravity[1];
     d.gz_acc = p.gravity[2];
     d.bmin = p.bound_min[0];
+    d.sparse_total = 96;   // gpu_model.cu:172-180
+    d.sparse_self = 15;
+    d.mid_total = 60;
     return d;
 }
 

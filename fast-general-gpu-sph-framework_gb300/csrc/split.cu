@@ -28,11 +28,11 @@ __device__ __forceinline__ int cell_n(const int32_t *__restrict__ start, int c) 
     return start[c + 1] - start[c];
 }
 
-// A6: SMS task count of one cell (gpu_model.cu:137-181, same thresholds,
-// same neighbour bounds tests).
+// A6: SMS task count of one cell (gpu_model.cu:137-181, same neighbour
+// bounds tests; the thresholds are the reference's unless tuned).
 __global__ void __launch_bounds__(256)
 k_cell_model(const int32_t *__restrict__ occ, const Counters *ctr,
-             const int32_t *__restrict__ start, SceneTable T,
+             const int32_t *__restrict__ start, SceneTable T, int3 thr,
              int4 *__restrict__ val) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= ctr->num_occ) return;
@@ -53,9 +53,9 @@ k_cell_model(const int32_t *__restrict__ occ, const Counters *ctr,
     if (idx >= slice) totaln += cell_n(start, gidx - slice);
     if (idx + slice < numc) totaln += cell_n(start, gidx + slice);
     int req;
-    if (totaln < 96 && self < 15)
+    if (totaln < thr.x && self < thr.y)     // reference: 96, 15
         req = 0;
-    else if (totaln < 60)
+    else if (totaln < thr.z)                // reference: 60
         req = (self + 27) >> 5;
     else
         req = (self + 31) >> 5;
@@ -305,8 +305,9 @@ void launch_split(const Frame &f, const DevParams &P, int max_occ,
                   cudaStream_t s) {
     if (f.n <= 0 || max_occ <= 0) return;
     const int blocks256 = (max_occ + 255) / 256;
-    k_cell_model<<<blocks256, 256, 0, s>>>(f.occ_list, f.ctr, f.cell_start,
-                                          f.scenes, f.cell_val);
+    k_cell_model<<<blocks256, 256, 0, s>>>(
+        f.occ_list, f.ctr, f.cell_start, f.scenes,
+        make_int3(P.sparse_total, P.sparse_self, P.mid_total), f.cell_val);
     const int ntiles = (max_occ + kScanTile - 1) / kScanTile;
     k_val_scan_reduce<<<ntiles, kScanThreads, 0, s>>>(f.cell_val, f.ctr,
                                                      f.scan_tiles4);

@@ -101,6 +101,7 @@ struct System {
     bool lists_valid = false;   // TRA neighbour masks match the state
     uint64_t frames = 0;
 
+    LaunchShape shape = kMaxShape;   // CTAs per SM of the density/force kernels
     int graph_frames = 0;   // frames per captured CUDA graph (0: stream launches)
     cudaGraphExec_t graph[2] = {nullptr, nullptr};   // by starting parity
 
@@ -274,9 +275,7 @@ struct System {
                 (st = alloc_n(&ev[b], N)))
                 return st;
         }
-        if ((st = alloc_n(&acc, N)) || (st = alloc_n(&fr.sx, N + 2)) ||
-            (st = alloc_n(&fr.sy, N + 2)) || (st = alloc_n(&fr.sz, N + 2)) ||
-            (st = alloc_n(&fr.key_in, N)) ||
+        if ((st = alloc_n(&acc, N)) || (st = alloc_n(&fr.key_in, N)) ||
             (st = alloc_n(&fr.slot, N)) || (st = alloc_n(&fr.pairs, N)) ||
             (st = alloc_n(&fr.key, N)) || (st = alloc_n(&fr.perm, N)) ||
             (st = alloc_n(&fr.cell_count, C)) ||
@@ -312,8 +311,6 @@ struct System {
             GSPH_CUDA(cudaMemsetAsync(ev[b], 0, sizeof(float4) * N, stream));
         }
         GSPH_CUDA(cudaMemsetAsync(acc, 0, sizeof(float4) * N, stream));
-        for (float *a : {fr.sx, fr.sy, fr.sz})
-            GSPH_CUDA(cudaMemsetAsync(a, 0, sizeof(float) * (N + 2), stream));
         if (n > 0) {
             GSPH_CUDA(cudaMemcpyAsync(pos[0], pos4, sizeof(float4) * n,
                                       cudaMemcpyHostToDevice, stream));
@@ -457,11 +454,11 @@ struct System {
         launch_split(f, dp, max_occ, stream);
     }
     void enqueue_density(int b) {
-        launch_density(frame_physics(b), dp, num_sms, stream);
+        launch_density(frame_physics(b), dp, num_sms, shape, stream);
         lists_valid = true;
     }
     void enqueue_force(int b) {
-        launch_force(frame_physics(b), dp, num_sms, lists_valid, stream);
+        launch_force(frame_physics(b), dp, num_sms, lists_valid, shape, stream);
     }
     void enqueue_advance(int b) {
         launch_integrate(frame_physics(b), dp, stream);
@@ -609,6 +606,134 @@ struct System {
         uint32_t z[2] = {0, 0};
         cudaMemcpyAsync(&fr.ctr->err, z, sizeof(z), cudaMemcpyHostToDevice, stream);
         cudaStreamSynchronize(stream);
+    }
+
+    gsph_tuning tuning() const {
+        gsph_tuning t{};
+        t.sparse_total = dp.sparse_total;
+        t.sparse_self = dp.sparse_self;
+        t.mid_total = dp.mid_total;
+        t.ctas_density_tra = shape.density_tra;
+        t.ctas_density_sms = shape.density_sms;
+        t.ctas_force_tra = shape.force_tra;
+        t.ctas_force_sms = shape.force_sms;
+        return t;
+    }
+
+    gsph_status set_tuning(const gsph_tuning &t) {
+        if (t.sparse_total < 0 || t.sparse_self < 0 || t.mid_total < 0 ||
+            t.ctas_density_tra < 1 || t.ctas_density_tra > kMaxShape.density_tra ||
+            t.ctas_density_sms < 1 || t.ctas_density_sms > kMaxShape.density_sms ||
+            t.ctas_force_tra < 1 || t.ctas_force_tra > kMaxShape.force_tra ||
+            t.ctas_force_sms < 1 || t.ctas_force_sms > kMaxShape.force_sms) {
+            set_error("gsph_set_tuning: thresholds must be >= 0 and CTAs per SM in "
+                      "[1, %d/%d/%d/%d]", kMaxShape.density_tra, kMaxShape.density_sms,
+                      kMaxShape.force_tra, kMaxShape.force_sms);
+            return GSPH_ERR_INVALID_ARG;
+        }
+        dp.sparse_total = t.sparse_total;
+        dp.sparse_self = t.sparse_self;
+        dp.mid_total = t.mid_total;
+        shape = {t.ctas_density_tra, t.ctas_density_sms, t.ctas_force_tra,
+                 t.ctas_force_sms};
+        drop_graphs();   // the captured launches carry the old values
+        return GSPH_OK;
+    }
+
+    // Times each candidate on a saved copy of the current state (one warm-up
+    // frame, then `trial` frames between events), restores the state after
+    // every trial and installs the fastest candidate.
+    gsph_status autotune(int trial, const gsph_tuning *cand, int nc, gsph_tuning *best,
+                         float *best_ms) {
+        if (trial < 1 || nc < 1 || !cand) {
+            set_error("gsph_autotune: need frames_per_trial >= 1 and a candidate");
+            return GSPH_ERR_INVALID_ARG;
+        }
+        for (int k = 0; k < nc; ++k) {
+            gsph_tuning probe = cand[k];
+            const gsph_tuning keep = tuning();
+            gsph_status st = set_tuning(probe);
+            set_tuning(keep);
+            if (st) return st;
+        }
+        GSPH_CUDA(cudaStreamSynchronize(stream));
+        const gsph_tuning start = tuning();
+        if (numc == 0 || n == 0) {
+            if (best) *best = start;
+            if (best_ms) *best_ms = 0.f;
+            return GSPH_OK;
+        }
+        const size_t bytes = sizeof(float4) * size_t(n);
+        float4 *saved = nullptr;
+        GSPH_CUDA(cudaMalloc(&saved, 3 * bytes));
+        const int cur0 = cur;
+        const uint64_t frames0 = frames;
+        const bool arranged0 = arranged, grid0 = grid_current;
+        const int graphs0 = graph_frames;
+        const bool timing0 = timing;
+        auto restore = [&]() -> gsph_status {
+            cur = cur0;
+            GSPH_CUDA(cudaMemcpyAsync(pos[cur], saved, bytes, cudaMemcpyDeviceToDevice, stream));
+            GSPH_CUDA(cudaMemcpyAsync(vel[cur], saved + n, bytes, cudaMemcpyDeviceToDevice,
+                                      stream));
+            GSPH_CUDA(cudaMemcpyAsync(ev[cur], saved + 2 * size_t(n), bytes,
+                                      cudaMemcpyDeviceToDevice, stream));
+            return GSPH_OK;
+        };
+        gsph_status st = GSPH_OK;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        int best_k = -1;
+        float best_t = 0.f;
+        do {
+            cudaError_t ce = cudaMemcpyAsync(saved, pos[cur], bytes, cudaMemcpyDeviceToDevice,
+                                             stream);
+            if (ce == cudaSuccess)
+                ce = cudaMemcpyAsync(saved + n, vel[cur], bytes, cudaMemcpyDeviceToDevice,
+                                     stream);
+            if (ce == cudaSuccess)
+                ce = cudaMemcpyAsync(saved + 2 * size_t(n), ev[cur], bytes,
+                                     cudaMemcpyDeviceToDevice, stream);
+            if (ce == cudaSuccess) ce = cudaEventCreate(&e0);
+            if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+            if (ce != cudaSuccess) {
+                set_error("gsph_autotune: %s", cudaGetErrorString(ce));
+                st = GSPH_ERR_CUDA;
+                break;
+            }
+            graph_frames = 0;
+            timing = false;
+            for (int k = 0; k < nc && !st; ++k) {
+                if ((st = restore()) || (st = set_tuning(cand[k])) || (st = tick())) break;
+                cudaEventRecord(e0, stream);
+                for (int f = 0; f < trial && !st; ++f) st = tick();
+                cudaEventRecord(e1, stream);
+                if (st || (st = sync_and_check())) break;
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                ms /= float(trial);
+                if (best_k < 0 || ms < best_t) {
+                    best_k = k;
+                    best_t = ms;
+                }
+            }
+        } while (false);
+        gsph_status rs = restore();
+        set_tuning(best_k >= 0 && !st ? cand[best_k] : start);
+        frames = frames0;
+        arranged = arranged0;
+        grid_current = grid0;
+        lists_valid = false;
+        graph_frames = graphs0;
+        timing = timing0;
+        cudaStreamSynchronize(stream);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        cudaFree(saved);
+        if (st) return st;
+        if (rs) return rs;
+        if (best) *best = cand[best_k];
+        if (best_ms) *best_ms = best_t;
+        return GSPH_OK;
     }
 
     gsph_status stage_times(float out[4]) {
@@ -1273,6 +1398,79 @@ gsph_status gsph_snapshot_load(const char *path, int device, gsph_handle *out) {
     s.frames = frames;
     *out = h;
     return GSPH_OK;
+}
+
+gsph_status gsph_tuning_default(gsph_tuning *out) {
+    if (!out) {
+        set_error("gsph_tuning_default: null output");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    *out = gsph_tuning{};
+    out->sparse_total = 96;   // gpu_model.cu:172-180
+    out->sparse_self = 15;
+    out->mid_total = 60;
+    out->ctas_density_tra = kMaxShape.density_tra;
+    out->ctas_density_sms = kMaxShape.density_sms;
+    out->ctas_force_tra = kMaxShape.force_tra;
+    out->ctas_force_sms = kMaxShape.force_sms;
+    return GSPH_OK;
+}
+
+gsph_status gsph_get_tuning(gsph_handle h, gsph_tuning *out) {
+    if (!h || !out) {
+        set_error("gsph_get_tuning: null argument");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    *out = h->sys.tuning();
+    return GSPH_OK;
+}
+
+gsph_status gsph_set_tuning(gsph_handle h, const gsph_tuning *t) {
+    gsph_status st = check_handle(h);
+    if (st) return st;
+    if (!t) {
+        set_error("gsph_set_tuning: null tuning");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    GSPH_CUDA(cudaStreamSynchronize(h->sys.stream));
+    return h->sys.set_tuning(*t);
+}
+
+// Built-in candidates: four split-threshold sets (the reference's, all TRA,
+// SMS-leaning, TRA-leaning) x two CTA counts for each TRA pass.
+static std::vector<gsph_tuning> default_candidates() {
+    std::vector<gsph_tuning> c;
+    const int thr[4][3] = {{96, 15, 60}, {0x7FFFFFFF, 0x7FFFFFFF, 60},
+                           {48, 8, 30}, {192, 30, 120}};
+    for (const auto &t : thr)
+        for (int dt : {kMaxShape.density_tra, kMaxShape.density_tra - 2})
+            for (int ft : {kMaxShape.force_tra, kMaxShape.force_tra - 1}) {
+                gsph_tuning g{};
+                g.sparse_total = t[0];
+                g.sparse_self = t[1];
+                g.mid_total = t[2];
+                g.ctas_density_tra = dt;
+                g.ctas_density_sms = kMaxShape.density_sms;
+                g.ctas_force_tra = ft;
+                g.ctas_force_sms = kMaxShape.force_sms;
+                c.push_back(g);
+            }
+    return c;
+}
+
+gsph_status gsph_autotune(gsph_handle h, int frames_per_trial,
+                          const gsph_tuning *candidates, int n_candidates,
+                          gsph_tuning *best_out, float *best_ms_out) {
+    gsph_status st = check_handle(h);
+    if (st) return st;
+    std::vector<gsph_tuning> builtin;
+    if (!candidates) {
+        builtin = default_candidates();
+        candidates = builtin.data();
+        n_candidates = int(builtin.size());
+    }
+    return h->sys.autotune(frames_per_trial, candidates, n_candidates, best_out,
+                           best_ms_out);
 }
 
 gsph_status gsph_checksum(gsph_handle h, double out[5]) {

@@ -142,6 +142,20 @@ typedef struct {
     double particle_steps_per_s;
 } gsph_bench_report;
 
+/* Tunables of the TRA/SMS split and of the density/force launches. The
+ * defaults (gsph_tuning_default) are the reference's performance model
+ * (gpu_model.cu:172-180: a cell stays TRA while its 7-cell total is below
+ * sparse_total and its own count below sparse_self; below mid_total it gets
+ * (n+27)>>5 SMS tasks, else (n+31)>>5) and this library's launch shapes (CTAs
+ * per SM of each pass, at most 6 / 6 / 4 / 4). Other thresholds change which
+ * cells take the SMS path: results stay within the parity tolerances but the
+ * split is no longer the reference's. */
+typedef struct {
+    int32_t sparse_total, sparse_self, mid_total;
+    int32_t ctas_density_tra, ctas_density_sms, ctas_force_tra, ctas_force_sms;
+    int32_t reserved_;
+} gsph_tuning;
+
 /* Fields for gsph_copy_out / gsph_copy_in. All particle fields are in the
  * handle's current (sorted) order. */
 typedef enum {
@@ -275,6 +289,21 @@ gsph_status gsph_copy_in_async(gsph_handle h, gsph_field field,
                                const void *host_src, size_t bytes);
 gsph_status gsph_copy_out_async(gsph_handle h, gsph_field field,
                                 void *host_dst, size_t bytes);
+
+/* Split thresholds and launch shapes (see gsph_tuning). */
+gsph_status gsph_tuning_default(gsph_tuning *out);
+gsph_status gsph_get_tuning(gsph_handle h, gsph_tuning *out);
+gsph_status gsph_set_tuning(gsph_handle h, const gsph_tuning *t);
+/* Times n_candidates tunings (NULL: a built-in grid of split thresholds and
+ * CTAs per SM) on the handle's current state, frames_per_trial frames each
+ * after one warm-up frame, restoring the state after every trial, and
+ * installs the fastest. best_out / best_ms_out (either may be NULL) receive
+ * it and its device time per frame. The state, frame counter and results of
+ * the handle are as before the call. Replaces the reference's fixed
+ * thresholds; no counterpart in the reference. */
+gsph_status gsph_autotune(gsph_handle h, int frames_per_trial,
+                          const gsph_tuning *candidates, int n_candidates,
+                          gsph_tuning *best_out, float *best_ms_out);
 
 /* FP64 state checksum as the reference's benchmark prints it:
  * {sum x, sum y, sum z, sum w, sum ((i&1023)+1)*(x+3y+7z)}. */
