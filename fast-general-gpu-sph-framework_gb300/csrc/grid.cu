@@ -245,6 +245,26 @@ __device__ __forceinline__ uint32_t pack_xslab(int s1, int s2, int s3, int cnt) 
     return uint32_t(s1) | (uint32_t(s2) << 10) | (uint32_t(s3) << 20);
 }
 
+// Writes the 16 (micro-x, micro-z) group offsets of a cell from its group
+// counts, and the three micro-x slab boundaries derived from them.
+__device__ __forceinline__ void write_groups(const Frame &f, uint32_t cell,
+                                             const int (&n16)[16], int cnt) {
+    int off[17];
+    off[0] = 0;
+#pragma unroll
+    for (int g = 0; g < 16; ++g) off[g + 1] = off[g] + n16[g];
+    f.cell_xslab[cell] = pack_xslab(off[4], off[8], off[12], cnt);
+    if (!f.cell_grp) return;
+    uint32_t w[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        w[k] = uint32_t(off[2 * k] & 0xFFFF) | (uint32_t(off[2 * k + 1] & 0xFFFF) << 16);
+    if (cnt > 65535) w[0] = (w[0] & 0xFFFF0000u) | kGroupsUnknown;
+    uint4 *dst = reinterpret_cast<uint4 *>(f.cell_grp + size_t(cell) * 16);
+    dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
+    dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
+}
+
 __device__ __forceinline__ void move_particle(const Frame &f, int dst,
                                               unsigned long long e) {
     const int src = int(e & 0xFFFFFFFFull);
@@ -269,14 +289,22 @@ __global__ void __launch_bounds__(256) k_sort_small(Frame f) {
     for (int j = 0; j < cnt; ++j) rank += (f.pairs[b + j] < e) ? 1 : 0;
     move_particle(f, b + rank, e);
     if (rank == 0) {
-        int s1 = 0, s2 = 0, s3 = 0;
+        // group counts, 8 bits each (cnt <= 32), packed in two words
+        unsigned long long lo = 0, hi = 0;
         for (int j = 0; j < cnt; ++j) {
-            const int x = int((f.pairs[b + j] >> 36) & 3ull);
-            s1 += x < 1;
-            s2 += x < 2;
-            s3 += x < 3;
+            const int g = int((f.pairs[b + j] >> 34) & 15ull);
+            if (g < 8)
+                lo += 1ull << (8 * g);
+            else
+                hi += 1ull << (8 * (g - 8));
         }
-        f.cell_xslab[cell] = pack_xslab(s1, s2, s3, cnt);
+        int n16[16];
+#pragma unroll
+        for (int g = 0; g < 8; ++g) {
+            n16[g] = int((lo >> (8 * g)) & 0xFF);
+            n16[g + 8] = int((hi >> (8 * g)) & 0xFF);
+        }
+        write_groups(f, cell, n16, cnt);
         f.cell_count[cell] = 0;   // ready for the next frame's atomics
     }
 }
@@ -285,35 +313,31 @@ __global__ void __launch_bounds__(256) k_sort_small(Frame f) {
 // in shared memory (global memory beyond kBigCellSmem), rank by counting.
 __global__ void __launch_bounds__(256) k_sort_big(Frame f) {
     __shared__ unsigned long long sp[kBigCellSmem];
-    __shared__ int slab[3];
+    __shared__ int grp[16];
     const int nbig = f.ctr->num_big;
     for (int q = blockIdx.x; q < nbig; q += gridDim.x) {
         const int cell = f.big_list[q];
         const int b = f.cell_start[cell];
         const int cnt = f.cell_start[cell + 1] - b;
         const bool in_smem = cnt <= kBigCellSmem;
-        if (threadIdx.x < 3) slab[threadIdx.x] = 0;
+        if (threadIdx.x < 16) grp[threadIdx.x] = 0;
         if (in_smem)
             for (int j = threadIdx.x; j < cnt; j += blockDim.x) sp[j] = f.pairs[b + j];
         __syncthreads();
         const unsigned long long *src = in_smem ? sp : f.pairs + b;
-        int c1 = 0, c2 = 0, c3 = 0;
         for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
             const unsigned long long e = src[i];
             int rank = 0;
             for (int j = 0; j < cnt; ++j) rank += (src[j] < e) ? 1 : 0;
             move_particle(f, b + rank, e);
-            const int x = int((e >> 36) & 3ull);
-            c1 += x < 1;
-            c2 += x < 2;
-            c3 += x < 3;
+            atomicAdd(&grp[int((e >> 34) & 15ull)], 1);
         }
-        atomicAdd(&slab[0], c1);
-        atomicAdd(&slab[1], c2);
-        atomicAdd(&slab[2], c3);
         __syncthreads();
         if (threadIdx.x == 0) {
-            f.cell_xslab[cell] = pack_xslab(slab[0], slab[1], slab[2], cnt);
+            int n16[16];
+#pragma unroll
+            for (int g = 0; g < 16; ++g) n16[g] = grp[g];
+            write_groups(f, uint32_t(cell), n16, cnt);
             f.cell_count[cell] = 0;
         }
         __syncthreads();

@@ -27,6 +27,7 @@ constexpr int kBigCellSmem = 4096;
 constexpr int kSmsTaskParticles = 32;
 // Sentinel for cell_xslab: slab boundaries unknown, search the whole cell.
 constexpr uint32_t kXslabUnknown = 0xFFFFFFFFu;
+constexpr uint16_t kGroupsUnknown = 0xFFFFu;
 // Neighbour masks of TRA particles: the density pass records, for each of the
 // 9 neighbour rows of a TRA particle, a 32-bit mask of which candidates of the
 // row interact; the force pass walks the set bits instead of re-testing every
@@ -127,12 +128,21 @@ struct Frame {
     SceneTable scenes;
     const float4 *pos_in, *vel_in, *ev_in;     // unsorted (previous order)
     float4 *pos, *vel, *ev, *acc;              // sorted (current order)
+    // When set, the force pass also integrates each particle (the reference's
+    // advance) and writes the new state here instead of leaving it to a
+    // separate integration launch; the arrays must not alias pos/vel/ev.
+    float4 *pos_next, *vel_next, *ev_next;
     uint32_t *key_in, *slot;                   // per source particle
     unsigned long long *pairs;                 // (key << 32 | src), by cell
     uint32_t *key;                             // sorted keys
     int32_t *perm;                             // source of each sorted slot
     int32_t *cell_count, *cell_start;
     uint32_t *cell_xslab;
+    // Per cell, 16 offsets (relative to the cell start) of the first particle
+    // of each (micro-x, micro-z) group, group g = mx * 4 + mz, in sort order;
+    // entry 0 is kGroupsUnknown for cells above 65,535 particles. Null when the
+    // caller does not keep it.
+    uint16_t *cell_grp;
     int32_t *occ_list, *big_list;
     int4 *cell_val;                            // per occupied cell {req,sms,tra}
     int4 *cell_prefix;                         // exclusive prefix of cell_val
@@ -163,7 +173,7 @@ void launch_split(const Frame &f, const DevParams &P, int max_occ,
 struct LaunchShape {
     int density_tra, density_sms, force_tra, force_sms;
 };
-constexpr LaunchShape kMaxShape = {6, 6, 4, 4};   // the kernels' launch bounds
+constexpr LaunchShape kMaxShape = {6, 5, 4, 4};   // the kernels' launch bounds
 
 void launch_density(const Frame &f, const DevParams &P, int num_sms,
                     const LaunchShape &shape, cudaStream_t s);

@@ -142,8 +142,73 @@ __device__ __forceinline__ void write_density(const Frame &f, const DevParams &P
     f.ev[self].w = (powf_7(rho * P.inv_rest_density) - 1) * P.gas_constant;
 }
 
+// knIntegrateVelocityE (integration_kernels.cu:235-336), same operation order:
+// penalty walls on the old velocity, a = F/rho + g, clamps, semi-implicit
+// Euler, damped reflection, ev = (v_new + ev_old) / 2; 1/rho and pressure
+// are kept.
+__device__ __forceinline__ void integrate_one(const float4 tp, const float4 v4,
+                                              const float4 ev, float ax, float ay,
+                                              float az, const DevParams &P,
+                                              const SceneGeom &G, float4 &pos_out,
+                                              float4 &vel_out, float4 &ev_out) {
+    float vx = v4.x, vy = v4.y, vz = v4.z;
+    const float alpha = 20000000.f;
+    const float beta = 200000.f;
+    const float kernel = P.wall_kernel;
+    float diff;
+    diff = kernel - (tp.y - P.bmin);
+    if (diff > 0.0f) ay += alpha * diff - beta * vy;
+    diff = kernel - (G.bmax_y - tp.y);
+    if (diff > 0.0f) ay -= alpha * diff + beta * vy;
+    diff = kernel - (tp.x - P.bmin);
+    if (diff > 0.0f) ax += alpha * diff - beta * vx;
+    diff = kernel - (G.bmax_x - tp.x);
+    if (diff > 0.0f) ax -= alpha * diff + beta * vx;
+    diff = kernel - (tp.z - P.bmin);
+    if (diff > 0.0f) az += alpha * diff - beta * vz;
+    diff = kernel - (G.bmax_z - tp.z);
+    if (diff > 0.0f) az -= alpha * diff + beta * vz;
+    const float acc_limit = 3000000.f;
+    const float vel_limit = 36.f;
+    ax = ax * tp.w + P.gx_acc;
+    ay = ay * tp.w + P.gy_acc;
+    az = az * tp.w + P.gz_acc;
+    float speed = ax * ax + ay * ay + az * az;
+    if (speed > acc_limit) {
+        const float s = sqrtf(acc_limit / speed);
+        ax *= s;
+        ay *= s;
+        az *= s;
+    }
+    vx += ax * P.time_step;
+    vy += ay * P.time_step;
+    vz += az * P.time_step;
+    speed = vx * vx + vy * vy + vz * vz;
+    if (speed > vel_limit) {
+        const float s = sqrtf(vel_limit / speed);
+        vx *= s;
+        vy *= s;
+        vz *= s;
+    }
+    float px = tp.x + vx * P.time_step;
+    float py = tp.y + vy * P.time_step;
+    float pz = tp.z + vz * P.time_step;
+    if (px >= G.bmax_x) { vx *= P.wall_damping; px = G.bmax_x - kernel; }
+    if (px <= P.bmin) { vx *= P.wall_damping; px = P.bmin + kernel; }
+    if (py >= G.bmax_y) { vy *= P.wall_damping; py = G.bmax_y - kernel; }
+    if (py <= P.bmin) { vy *= P.wall_damping; py = P.bmin + kernel; }
+    if (pz >= G.bmax_z) { vz *= P.wall_damping; pz = G.bmax_z - kernel; }
+    if (pz <= P.bmin) { vz *= P.wall_damping; pz = P.bmin + kernel; }
+    pos_out = make_float4(px, py, pz, tp.w);
+    vel_out = make_float4(vx, vy, vz, 0.f);
+    ev_out = make_float4((vx + ev.x) * 0.5f, (vy + ev.y) * 0.5f, (ev.z + vz) * 0.5f, ev.w);
+}
+
+// Writes the force; with f.pos_next set, also integrates the particle (the
+// same arithmetic as k_integrate on the stored force) into the next buffers.
 __device__ __forceinline__ void write_force(const Frame &f, const DevParams &P,
-                                            int self, float inv_rho,
+                                            int self, const float4 &p,
+                                            const float4 &pev, const SceneGeom &G,
                                             const ForceAcc &a, bool sms) {
     float tx = a.px * P.half_spiky + a.vx * P.visco_coef;
     float ty = a.py * P.half_spiky + a.vy * P.visco_coef;
@@ -152,7 +217,7 @@ __device__ __forceinline__ void write_force(const Frame &f, const DevParams &P,
     const float gy = a.gy * P.grad_color_scale;
     const float gz = a.gz * P.grad_color_scale;
     float lap = a.lap * P.lplc_color_scale;
-    lap *= inv_rho;
+    lap *= p.w;   // 1/rho_i
     float sx = 0.f, sy = 0.f, sz = 0.f;
     const float n2 = gx * gx + gy * gy + gz * gz;
     if (sms) {
@@ -177,7 +242,15 @@ __device__ __forceinline__ void write_force(const Frame &f, const DevParams &P,
     tx *= P.mass;
     ty *= P.mass;
     tz *= P.mass;
-    f.acc[self] = make_float4(tx + sx, ty + sy, tz + sz, 0.f);
+    const float4 acc = make_float4(tx + sx, ty + sy, tz + sz, 0.f);
+    f.acc[self] = acc;
+    if (f.pos_next) {
+        float4 po, vo, eo;
+        integrate_one(p, f.vel[self], pev, acc.x, acc.y, acc.z, P, G, po, vo, eo);
+        f.pos_next[self] = po;
+        f.vel_next[self] = vo;
+        f.ev_next[self] = eo;
+    }
 }
 
 // Squared distances to staged candidates 2k and 2k+1 (x/y/z arrays), as a
@@ -258,34 +331,122 @@ k_density_tra(Frame f, DevParams P) {
     }
 }
 
-// Stage candidates [base, base + cnt) of the sorted arrays into a warp's
-// shared arrays (two per lane); slots past cnt get far-away padding.
-__device__ __forceinline__ void stage_xyz(const Frame &f, int base, int cnt,
-                                          float *sx, float *sy, float *sz,
-                                          float4 *sp, float4 *sv, int lane) {
-#pragma unroll
-    for (int h = 0; h < kSmsBatch; h += 32) {
-        const int t = h + lane;
-        float4 q = make_float4(kFar, kFar, kFar, 0.f);
-        float4 qv = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (t < cnt) {
-            q = f.pos[base + t];
-            if (sv) qv = f.ev[base + t];
-        }
-        sx[t] = q.x;
-        sy[t] = q.y;
-        sz[t] = q.z;
-        if (sp) sp[t] = q;
-        if (sv) sv[t] = qv;
+// ------------------------------------------------------- SMS candidates --
+// The candidates of an SMS task, row by row (rows z-major as in the
+// reference), each row in increasing sorted index. Rows at dz = 0 are the
+// reference's x-merged range (micro-x slabs pruned by the task's x bounds,
+// kernel_common.cuh:614-674). Rows at dz = -1 / +1 are further pruned in z: a
+// particle of the cell below (above) whose micro-z is below (above) every
+// task particle's own micro-z is at least h away from all of them, so only
+// the micro-z groups [zmin, 3] ([0, zmax]) of each micro-x slab are kept,
+// using the per-cell (micro-x, micro-z) group offsets of the sort. Pruned
+// candidates never interact, so the interacting set and its order are the
+// same as the reference's.
+//
+// Segment of lane l (< 12) of row cell m: cell m - 1 + l / 4, micro-x slab
+// l % 4, micro-z groups [zlo, zhi]; empty where the slab is outside the
+// task's x bounds or the cell outside the grid. A cell whose groups are
+// unknown (> 65,535 particles) is taken whole by its first lane.
+__device__ __forceinline__ void sms_segment(const Frame &f, const SceneGeom &G, int m,
+                                            int cx, int xlo, int xhi, int zlo,
+                                            int zhi, int lane, int &sb, int &sl) {
+    sb = 0;
+    sl = 0;
+    if (lane >= 12) return;
+    const int k = lane >> 2, mx = lane & 3;
+    if (k == 0 && (cx == 0 || mx < xlo)) return;
+    if (k == 2 && (cx + 1 >= G.gx || mx > xhi)) return;
+    const int c = m + k - 1;
+    const int cs = f.cell_start[c];
+    const int cnt = f.cell_start[c + 1] - cs;
+    if (cnt <= 0) return;
+    const uint16_t *g = f.cell_grp + size_t(c) * 16;
+    int b, e;
+    if (g[0] == kGroupsUnknown) {
+        if (mx != (k == 0 ? xlo : 0)) return;
+        b = k == 0 ? slab_begin(f, c, cs, cs + cnt, xlo) - cs : 0;
+        e = k == 2 ? slab_end(f, c, cs, cs + cnt, xhi) - cs : cnt;
+    } else {
+        b = g[mx * 4 + zlo];
+        e = zhi < 3 ? g[mx * 4 + zhi + 1] : (mx < 3 ? g[mx * 4 + 4] : cnt);
+        b = min(b, cnt);
+        e = min(e, cnt);
     }
+    if (e > b) {
+        sb = cs + b;
+        sl = e - b;
+    }
+}
+
+// Streams a task's candidates through a warp's 64-slot staging batch:
+// stage(slot, index) fills one slot, run(pairs) evaluates the staged slots
+// two at a time; batches run full except the last (its odd slot is padded
+// by pad(slot)). Control flow is warp-uniform.
+template <class Stage, class Pad, class Run>
+__device__ __forceinline__ void sms_stream(const Frame &f, const SceneGeom &G,
+                                           const gsph_block_task &task, int zmin,
+                                           int zmax, int lane, Stage stage, Pad pad,
+                                           Run run) {
+    const int cx = task.cell_pos[0], cy = task.cell_pos[1], cz = task.cell_pos[2];
+    int fill = 0;
+    auto take_range = [&](int b, int len) {
+        int o = 0;
+        while (o < len) {
+            const int n = min(len - o, kSmsBatch - fill);
+            for (int t = lane; t < n; t += 32) stage(fill + t, b + o + t);
+            fill += n;
+            o += n;
+            if (fill == kSmsBatch) {
+                __syncwarp();
+                run(kSmsBatch / 2);
+                __syncwarp();
+                fill = 0;
+            }
+        }
+    };
+    for (int r = 0; r < 9; ++r) {
+        const int ny = cy + (r % 3) - 1;
+        const int nz = cz + (r / 3) - 1;
+        if (ny < 0 || ny >= G.gy || nz < 0 || nz >= G.gz) continue;
+        const int m = G.cbase + cx + G.gx * (ny + G.gy * nz);
+        const int dz = r / 3 - 1;
+        const int zlo = dz < 0 ? zmin : 0, zhi = dz > 0 ? zmax : 3;
+        if ((zlo == 0 && zhi == 3) || !f.cell_grp) {
+            int begin, end;
+            row_range(f, G, m, cx, task.xxi, task.xxx, begin, end);
+            take_range(begin, end - begin);
+        } else {
+            int sb, sl;
+            sms_segment(f, G, m, cx, task.xxi, task.xxx, zlo, zhi, lane, sb, sl);
+            const unsigned nonempty = __ballot_sync(kFull, sl > 0);
+            for (unsigned w = nonempty; w; w &= w - 1) {
+                const int src = __ffs(w) - 1;
+                take_range(__shfl_sync(kFull, sb, src), __shfl_sync(kFull, sl, src));
+            }
+        }
+    }
+    if (fill > 0) {
+        if ((fill & 1) && lane == 0) pad(fill);
+        __syncwarp();
+        run((fill + 1) >> 1);
+        __syncwarp();
+    }
+}
+
+// Micro-z range of a task's particles (warp-wide; inactive lanes neutral).
+__device__ __forceinline__ void task_z_range(const Frame &f, int self, bool active,
+                                             int &zmin, int &zmax) {
+    const int mz = active ? int((f.key[self] >> 2) & 3u) : -1;
+    zmin = int(__reduce_min_sync(kFull, unsigned(active ? mz : 3)));
+    zmax = __reduce_max_sync(kFull, active ? mz : 0);
 }
 
 // ------------------------------------------------------------ density SMS --
 // One 32-particle task per warp (density_kernels.cu:368-565). Candidates are
-// staged 64 at a time as x/y/z arrays in shared memory; every lane evaluates
-// them two at a time with packed FP32x2 arithmetic (distances and h^2 - r^2
-// round exactly as the scalar form).
-__global__ void __launch_bounds__(kWarpsPerBlock * 32, 6)
+// streamed 64 at a time into x/y/z arrays in shared memory; every lane
+// evaluates them two at a time with packed FP32x2 arithmetic (distances and
+// h^2 - r^2 round exactly as the scalar form).
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
 k_density_sms(Frame f, DevParams P) {
     __shared__ __align__(16) float sms_x[kWarpsPerBlock][kSmsBatch];
     __shared__ __align__(16) float sms_y[kWarpsPerBlock][kSmsBatch];
@@ -305,26 +466,28 @@ k_density_sms(Frame f, DevParams P) {
         if (cb + int(task.p_offset) >= cend) continue;   // warp-uniform
         const float4 p = f.pos[active ? self : cend - 1];
         const SceneGeom G = geom_of_cell(f.scenes, task.cellid);
-        const int cx = task.cell_pos[0], cy = task.cell_pos[1],
-                  cz = task.cell_pos[2];
+        int zmin, zmax;
+        task_z_range(f, self, active, zmin, zmax);
         const float2 npx = make_float2(-p.x, -p.x);
         const float2 npy = make_float2(-p.y, -p.y);
         const float2 npz = make_float2(-p.z, -p.z);
         const float2 h2v = make_float2(P.h2, P.h2);
         const float2 m1 = make_float2(-1.f, -1.f);
         float2 acc = make_float2(0.f, 0.f);
-        for (int r = 0; r < 9; ++r) {
-            const int ny = cy + (r % 3) - 1;
-            const int nz = cz + (r / 3) - 1;
-            if (ny < 0 || ny >= G.gy || nz < 0 || nz >= G.gz) continue;
-            const int m = G.cbase + cx + G.gx * (ny + G.gy * nz);
-            int begin, end;
-            row_range(f, G, m, cx, task.xxi, task.xxx, begin, end);
-            for (int base = begin; base < end; base += kSmsBatch) {
-                const int cnt = min(kSmsBatch, end - base);
-                stage_xyz(f, base, cnt, sx, sy, sz, nullptr, nullptr, lane);
-                __syncwarp();
-                const int pairs = (cnt + 1) >> 1;
+        sms_stream(
+            f, G, task, zmin, zmax, lane,
+            [&](int slot, int j) {
+                const float4 q = f.pos[j];
+                sx[slot] = q.x;
+                sy[slot] = q.y;
+                sz[slot] = q.z;
+            },
+            [&](int slot) {
+                sx[slot] = kFar;
+                sy[slot] = kFar;
+                sz[slot] = kFar;
+            },
+            [&](int pairs) {
 #pragma unroll 4
                 for (int k = 0; k < pairs; ++k) {
                     const float2 d2 = pair_d2(sx, sy, sz, k, npx, npy, npz);
@@ -333,9 +496,7 @@ k_density_sms(Frame f, DevParams P) {
                     t.y = (t.y < 0.f || d2.y < kFloatSmall) ? 0.f : t.y;
                     acc = __ffma2_rn(__fmul2_rn(t, t), t, acc);
                 }
-                __syncwarp();
-            }
-        }
+            });
         if (active) write_density(f, P, self, acc.x + acc.y, true);
     }
 }
@@ -431,7 +592,7 @@ k_force_tra(Frame f, DevParams P, bool fresh) {
                 }
             }
         }
-        write_force(f, P, self, p.w, a, false);
+        write_force(f, P, self, p, pev, G, a, false);
     }
 }
 
@@ -553,13 +714,12 @@ k_force_sms(Frame f, DevParams P) {
             a.gy = -(Gy.x + Gy.y);
             a.gz = -(Gz.x + Gz.y);
             a.lap = L.x + L.y;
-            write_force(f, P, self, p.w, a, true);
+            write_force(f, P, self, p, pev, G, a, true);
         }
     }
 }
 
 // -------------------------------------------------------------- integrate --
-// knIntegrateVelocityE (integration_kernels.cu:235-336), same operation order.
 __global__ void __launch_bounds__(256)
 k_integrate(Frame f, DevParams P) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -569,59 +729,11 @@ k_integrate(Frame f, DevParams P) {
     const SceneGeom G = geom_of_particle(f.scenes, i);
     const float4 v4 = f.vel[i];
     const float4 a4 = f.acc[i];
-    float vx = v4.x, vy = v4.y, vz = v4.z;
-    float ax = a4.x, ay = a4.y, az = a4.z;
-    const float alpha = 20000000.f;
-    const float beta = 200000.f;
-    const float kernel = P.wall_kernel;
-    float diff;
-    diff = kernel - (tp.y - P.bmin);
-    if (diff > 0.0f) ay += alpha * diff - beta * vy;
-    diff = kernel - (G.bmax_y - tp.y);
-    if (diff > 0.0f) ay -= alpha * diff + beta * vy;
-    diff = kernel - (tp.x - P.bmin);
-    if (diff > 0.0f) ax += alpha * diff - beta * vx;
-    diff = kernel - (G.bmax_x - tp.x);
-    if (diff > 0.0f) ax -= alpha * diff + beta * vx;
-    diff = kernel - (tp.z - P.bmin);
-    if (diff > 0.0f) az += alpha * diff - beta * vz;
-    diff = kernel - (G.bmax_z - tp.z);
-    if (diff > 0.0f) az -= alpha * diff + beta * vz;
-    const float acc_limit = 3000000.f;
-    const float vel_limit = 36.f;
-    ax = ax * tp.w + P.gx_acc;
-    ay = ay * tp.w + P.gy_acc;
-    az = az * tp.w + P.gz_acc;
-    float speed = ax * ax + ay * ay + az * az;
-    if (speed > acc_limit) {
-        const float s = sqrtf(acc_limit / speed);
-        ax *= s;
-        ay *= s;
-        az *= s;
-    }
-    vx += ax * P.time_step;
-    vy += ay * P.time_step;
-    vz += az * P.time_step;
-    speed = vx * vx + vy * vy + vz * vz;
-    if (speed > vel_limit) {
-        const float s = sqrtf(vel_limit / speed);
-        vx *= s;
-        vy *= s;
-        vz *= s;
-    }
-    float px = tp.x + vx * P.time_step;
-    float py = tp.y + vy * P.time_step;
-    float pz = tp.z + vz * P.time_step;
-    if (px >= G.bmax_x) { vx *= P.wall_damping; px = G.bmax_x - kernel; }
-    if (px <= P.bmin) { vx *= P.wall_damping; px = P.bmin + kernel; }
-    if (py >= G.bmax_y) { vy *= P.wall_damping; py = G.bmax_y - kernel; }
-    if (py <= P.bmin) { vy *= P.wall_damping; py = P.bmin + kernel; }
-    if (pz >= G.bmax_z) { vz *= P.wall_damping; pz = G.bmax_z - kernel; }
-    if (pz <= P.bmin) { vz *= P.wall_damping; pz = P.bmin + kernel; }
-    f.pos[i] = make_float4(px, py, pz, tp.w);
-    f.vel[i] = make_float4(vx, vy, vz, 0.f);
-    f.ev[i] = make_float4((vx + ev.x) * 0.5f, (vy + ev.y) * 0.5f,
-                          (ev.z + vz) * 0.5f, ev.w);
+    float4 po, vo, eo;
+    integrate_one(tp, v4, ev, a4.x, a4.y, a4.z, P, G, po, vo, eo);
+    f.pos[i] = po;
+    f.vel[i] = vo;
+    f.ev[i] = eo;
 }
 
 // ------------------------------------------------------- FP64 reductions --

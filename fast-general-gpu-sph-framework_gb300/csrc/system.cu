@@ -281,6 +281,7 @@ struct System {
             (st = alloc_n(&fr.cell_count, C)) ||
             (st = alloc_n(&fr.cell_start, C + 1)) ||
             (st = alloc_n(&fr.cell_xslab, C)) ||
+            (st = alloc_n(&fr.cell_grp, C * 16)) ||
             (st = alloc_n(&fr.occ_list, size_t(occ_cap))) ||
             (st = alloc_n(&fr.big_list, size_t(occ_cap))) ||
             (st = alloc_n(&fr.cell_val, size_t(occ_cap))) ||
@@ -460,6 +461,17 @@ struct System {
     void enqueue_force(int b) {
         launch_force(frame_physics(b), dp, num_sms, lists_valid, shape, stream);
     }
+    // Force on buffer b with the integration fused in: the new state goes to
+    // buffer 1 - b (the previous frame's unsorted copy, no longer read), in
+    // buffer b's order.
+    void enqueue_force_advance(int b) {
+        Frame f = frame_physics(b);
+        f.pos_next = pos[1 - b];
+        f.vel_next = vel[1 - b];
+        f.ev_next = ev[1 - b];
+        launch_force(f, dp, num_sms, lists_valid, shape, stream);
+        lists_valid = false;
+    }
     void enqueue_advance(int b) {
         launch_integrate(frame_physics(b), dp, stream);
         lists_valid = false;
@@ -489,13 +501,10 @@ struct System {
     gsph_status build_graph(int parity) {
         cudaGraph_t g = nullptr;
         GSPH_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-        int in = parity;
         for (int k = 0; k < graph_frames; ++k) {
-            enqueue_arrange(in);
-            enqueue_density(1 - in);
-            enqueue_force(1 - in);
-            enqueue_advance(1 - in);
-            in = 1 - in;
+            enqueue_arrange(parity);
+            enqueue_density(1 - parity);
+            enqueue_force_advance(1 - parity);
         }
         cudaError_t e = cudaStreamEndCapture(stream, &g);
         if (e != cudaSuccess) {
@@ -521,7 +530,11 @@ struct System {
             }
     }
 
-    // One frame launched kernel by kernel (with stage events when timing).
+    // One frame launched kernel by kernel (with stage events when timing):
+    // the sort moves the state from buffer `cur` into the other buffer, and
+    // the force pass, which also integrates, writes the new state back into
+    // buffer `cur` in the sorted order. The integrate stage time is then 0
+    // (it is part of the force pass).
     gsph_status tick() {
         if (numc == 0) return GSPH_OK;   // a batch without scenes
         const int in = cur, out = 1 - cur;
@@ -534,16 +547,15 @@ struct System {
         if (timing) cudaEventRecord(evs[1], stream);
         enqueue_density(out);
         if (timing) cudaEventRecord(evs[2], stream);
-        enqueue_force(out);
-        if (timing) cudaEventRecord(evs[3], stream);
-        enqueue_advance(out);
+        enqueue_force_advance(out);
         if (timing) {
+            cudaEventRecord(evs[3], stream);
             cudaEventRecord(evs[4], stream);
             ev_pending.push_back(std::move(evs));
         }
         gsph_status st = check_launch();
         if (st) return st;
-        cur = out;
+        cur = in;
         arranged = true;
         grid_current = false;
         ++frames;
@@ -560,7 +572,6 @@ struct System {
                     if (st) return st;
                 }
                 GSPH_CUDA(cudaGraphLaunch(graph[cur], stream));
-                if (graph_frames & 1) cur = 1 - cur;
                 arranged = true;
                 grid_current = false;
                 lists_valid = false;

@@ -17,10 +17,12 @@ import time
 import numpy as np
 
 
-# Device bytes a scene holds in a batch: particle state, sort and split
-# workspace, neighbour masks (per particle) and cell tables (per cell).
-BYTES_PER_PARTICLE = 176
-BYTES_PER_CELL = 12
+# Device bytes a scene holds in a batch: particle state (two buffer sets),
+# force, sort and split workspace, neighbour masks and the occupied-cell lists
+# (bounded by the particle count) per particle; cell offsets, slab words and
+# group offsets per cell.
+BYTES_PER_PARTICLE = 221
+BYTES_PER_CELL = 44
 
 
 def scene_bytes(n_particles: int, n_cells: int) -> int:

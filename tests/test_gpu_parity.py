@@ -301,3 +301,28 @@ def test_grid_sort_dev_matches_handle(gsph, oracle, cuda_device):
                                 key.data_ptr(), perm.data_ptr(), cs.data_ptr(),
                                 base, nbytes - 256, stream)
     assert st == gsph.ERR_INVALID_ARG
+
+
+def test_step_equals_stage_sequence(gsph, scene):
+    """A frame of gsph_step (integration fused into the force pass) gives the
+    same bits as gsph_arrange, gsph_density, gsph_force and gsph_advance
+    called one by one (integration as its own launch)."""
+    name, p, pos = scene
+    rng = np.random.default_rng(9)
+    vel = np.zeros_like(pos)
+    vel[:, :3] = rng.normal(0.0, 0.3, (len(pos), 3))
+    fields = (gsph.FIELD_POSITION, gsph.FIELD_VELOCITY, gsph.FIELD_EVAL_VELOCITY,
+              gsph.FIELD_ACCELERATION, gsph.FIELD_KEY)
+    with make(gsph, p, pos, vel) as a, make(gsph, p, pos, vel) as b:
+        for _ in range(3):
+            a.step(1)
+            b.arrange()
+            b.density()
+            b.force()
+            b.advance()
+            for f in fields:
+                assert np.array_equal(a.copy_out(f).view(np.uint32),
+                                      b.copy_out(f).view(np.uint32)), (name, f)
+        with pytest.raises(gsph.GsphError) as ei:
+            b.density()                     # positions moved since the arrange
+        assert ei.value.status == gsph.ERR_STATE
