@@ -166,7 +166,7 @@ void launch_cell_scan(const Frame &f, const DevParams &P, cudaStream_t s);
 void launch_scatter_pairs(const Frame &f, cudaStream_t s);
 void launch_cell_sort(const Frame &f, int num_sms, cudaStream_t s);
 // ---- launchers (split.cu) ----
-void launch_split(const Frame &f, const DevParams &P, int max_occ,
+void launch_split(const Frame &f, const DevParams &P, int max_occ, int num_sms,
                   cudaStream_t s);
 // ---- launchers (physics.cu) ----
 // Launch shapes of the density and force passes: CTAs per SM of each kernel.

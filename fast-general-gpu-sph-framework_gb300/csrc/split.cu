@@ -16,6 +16,8 @@
 // particles, TRA particles} per occupied cell replaces the reference's second
 // counting sort, and no host synchronisation is needed: counts stay on the
 // device for the persistent density/force kernels.
+#include <algorithm>
+
 #include "gsph_internal.h"
 
 namespace gsph {
@@ -34,8 +36,9 @@ __global__ void __launch_bounds__(256)
 k_cell_model(const int32_t *__restrict__ occ, const Counters *ctr,
              const int32_t *__restrict__ start, SceneTable T, int3 thr,
              int4 *__restrict__ val) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= ctr->num_occ) return;
+    const int num_occ = ctr->num_occ;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < num_occ;
+         k += gridDim.x * blockDim.x) {
     const int gidx = occ[k];
     const SceneGeom G = geom_of_cell(T, gidx);
     const int idx = gidx - G.cbase;           // the scene's own cell index
@@ -61,6 +64,7 @@ k_cell_model(const int32_t *__restrict__ occ, const Counters *ctr,
         req = (self + 31) >> 5;
     const int sms = min(req * kSmsTaskParticles, self);
     val[k] = make_int4(req, sms, self - sms, 0);
+    }
 }
 
 __device__ __forceinline__ int4 add4(int4 a, int4 b) {
@@ -82,28 +86,29 @@ __global__ void __launch_bounds__(kScanThreads)
 k_val_scan_reduce(const int4 *__restrict__ in, const Counters *ctr,
                   int4 *__restrict__ tiles) {
     const int n = ctr->num_occ;
-    const int first = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
-    int4 s = make_int4(0, 0, 0, 0);
-    if (blockIdx.x * kScanTile < n) {
+    __shared__ int4 ws[kScanThreads / 32];
+    for (int tile = blockIdx.x; tile * kScanTile < n; tile += gridDim.x) {
+        const int first = tile * kScanTile + threadIdx.x * kScanItems;
+        int4 s = make_int4(0, 0, 0, 0);
 #pragma unroll 4
         for (int q = 0; q < kScanItems; ++q)
             if (first + q < n) s = add4(s, in[first + q]);
-    }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s = add4(s, shfl_down4(s, o));
-    __shared__ int4 ws[kScanThreads / 32];
-    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int4 t = make_int4(0, 0, 0, 0);
-        for (int w = 0; w < kScanThreads / 32; ++w) t = add4(t, ws[w]);
-        tiles[blockIdx.x] = t;
+        for (int o = 16; o > 0; o >>= 1) s = add4(s, shfl_down4(s, o));
+        if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int4 t = make_int4(0, 0, 0, 0);
+            for (int w = 0; w < kScanThreads / 32; ++w) t = add4(t, ws[w]);
+            tiles[tile] = t;
+        }
+        __syncthreads();
     }
 }
 
 __global__ void __launch_bounds__(1024)
-k_val_scan_tiles(int4 *__restrict__ tiles, int ntiles, Counters *ctr,
-                 int task_capacity) {
+k_val_scan_tiles(int4 *__restrict__ tiles, Counters *ctr, int task_capacity) {
+    const int ntiles = (ctr->num_occ + kScanTile - 1) / kScanTile;
     __shared__ int4 ws[32];
     __shared__ int4 carry;
     if (threadIdx.x == 0) carry = make_int4(0, 0, 0, 0);
@@ -155,8 +160,9 @@ __global__ void __launch_bounds__(kScanThreads)
 k_val_scan_apply(const int4 *__restrict__ in, const Counters *ctr,
                  const int4 *__restrict__ tiles, int4 *__restrict__ out) {
     const int n = ctr->num_occ;
-    if (blockIdx.x * kScanTile >= n) return;
-    const int first = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    __shared__ int4 ws[kScanThreads / 32];
+    for (int tile = blockIdx.x; tile * kScanTile < n; tile += gridDim.x) {
+    const int first = tile * kScanTile + threadIdx.x * kScanItems;
     int4 v[kScanItems];
     int4 s = make_int4(0, 0, 0, 0);
 #pragma unroll
@@ -171,16 +177,17 @@ k_val_scan_apply(const int4 *__restrict__ in, const Counters *ctr,
         int4 y = shfl_up4(x, o);
         if (lane >= o) x = add4(x, y);
     }
-    __shared__ int4 ws[kScanThreads / 32];
     if (lane == 31) ws[warp] = x;
     __syncthreads();
-    int4 run = tiles[blockIdx.x];
+    int4 run = tiles[tile];
     for (int w = 0; w < warp; ++w) run = add4(run, ws[w]);
     run = make_int4(run.x + x.x - s.x, run.y + x.y - s.y, run.z + x.z - s.z, 0);
 #pragma unroll
     for (int q = 0; q < kScanItems; ++q) {
         if (first + q < n) out[first + q] = run;
         run = add4(run, v[q]);
+    }
+    __syncthreads();
     }
 }
 
@@ -199,8 +206,9 @@ k_cell_emit(const int32_t *__restrict__ occ, const Counters *ctr,
             const int4 *__restrict__ val, const int4 *__restrict__ prefix,
             SceneTable T, int32_t *__restrict__ compact,
             gsph_block_task *__restrict__ tasks) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= ctr->num_occ) return;
+    const int num_occ = ctr->num_occ;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < num_occ;
+         k += gridDim.x * blockDim.x) {
     const int cell = occ[k];
     const int b = start[cell];
     const int n = start[cell + 1] - b;
@@ -210,7 +218,7 @@ k_cell_emit(const int32_t *__restrict__ occ, const Counters *ctr,
     const int task_count = ctr->task_count;
     for (int j = 0; j < v.z; ++j) compact[pre.z + j] = b + v.y + j;
     for (int j = 0; j < v.y; ++j) compact[middle + pre.y + j] = b + j;
-    if (v.x == 0) return;
+    if (v.x == 0) continue;
     const SceneGeom G = geom_of_cell(T, cell);
     const int local = cell - G.cbase;
     const uint16_t cx = uint16_t(local % G.gx);
@@ -257,15 +265,12 @@ k_cell_emit(const int32_t *__restrict__ occ, const Counters *ctr,
             pack_bounds(task.xxi, task.xxx, task.yyi, task.yyy, task.zzi, task.zzz);
         tasks[ti] = task;
     }
+    }
 }
 
-// A9: historical same-cell pairing of tasks (2k, 2k+1), odd-tail descriptor.
-__global__ void __launch_bounds__(128)
-k_judge(gsph_block_task *__restrict__ tasks, const Counters *ctr) {
-    const int pair = blockIdx.x * blockDim.x + threadIdx.x;
-    const int first = pair << 1;
-    const int task_count = ctr->task_count;
-    if (first >= task_count) return;
+// One pair (first, first + 1) of the historical same-cell pairing.
+__device__ __forceinline__ void judge_pair(gsph_block_task *__restrict__ tasks,
+                                           int first, int task_count) {
     const int second = first + 1;
     gsph_block_task a = tasks[first];
     if (second >= task_count) {
@@ -299,27 +304,37 @@ k_judge(gsph_block_task *__restrict__ tasks, const Counters *ctr) {
         pack_bounds(a.xxi, b.xxx, a.yyi, a.yyy, pmin_z, pmax_z);
 }
 
-}  // namespace
+// A9: historical same-cell pairing of tasks (2k, 2k+1), odd-tail descriptor.
+__global__ void __launch_bounds__(128)
+k_judge(gsph_block_task *__restrict__ tasks, const Counters *ctr) {
+    const int task_count = ctr->task_count;
+    for (int pair = blockIdx.x * blockDim.x + threadIdx.x; (pair << 1) < task_count;
+         pair += gridDim.x * blockDim.x)
+        judge_pair(tasks, pair << 1, task_count);
+}}  // namespace
 
-void launch_split(const Frame &f, const DevParams &P, int max_occ,
+void launch_split(const Frame &f, const DevParams &P, int max_occ, int num_sms,
                   cudaStream_t s) {
     if (f.n <= 0 || max_occ <= 0) return;
-    const int blocks256 = (max_occ + 255) / 256;
-    k_cell_model<<<blocks256, 256, 0, s>>>(
+    // grid-stride kernels over the device-side counts, sized for the capacity
+    // but at most a few CTAs per SM
+    const int cap256 = std::min((max_occ + 255) / 256, num_sms * 8);
+    const int cap128 = std::min((max_occ + 127) / 128, num_sms * 16);
+    const int ntiles = std::min((max_occ + kScanTile - 1) / kScanTile, num_sms * 4);
+    k_cell_model<<<cap256, 256, 0, s>>>(
         f.occ_list, f.ctr, f.cell_start, f.scenes,
         make_int3(P.sparse_total, P.sparse_self, P.mid_total), f.cell_val);
-    const int ntiles = (max_occ + kScanTile - 1) / kScanTile;
     k_val_scan_reduce<<<ntiles, kScanThreads, 0, s>>>(f.cell_val, f.ctr,
                                                      f.scan_tiles4);
-    k_val_scan_tiles<<<1, 1024, 0, s>>>(f.scan_tiles4, ntiles, f.ctr,
-                                       f.task_capacity);
+    k_val_scan_tiles<<<1, 1024, 0, s>>>(f.scan_tiles4, f.ctr, f.task_capacity);
     k_val_scan_apply<<<ntiles, kScanThreads, 0, s>>>(f.cell_val, f.ctr,
                                                     f.scan_tiles4, f.cell_prefix);
-    k_cell_emit<<<(max_occ + 127) / 128, 128, 0, s>>>(
+    k_cell_emit<<<cap128, 128, 0, s>>>(
         f.occ_list, f.ctr, f.cell_start, f.key, f.cell_val, f.cell_prefix,
         f.scenes, f.compact, f.tasks);
     const int max_pairs = (f.task_capacity + 1) / 2;
-    k_judge<<<(max_pairs + 127) / 128, 128, 0, s>>>(f.tasks, f.ctr);
+    k_judge<<<std::min((max_pairs + 127) / 128, num_sms * 8), 128, 0, s>>>(f.tasks,
+                                                                          f.ctr);
 }
 
 }  // namespace gsph

@@ -452,7 +452,7 @@ struct System {
         launch_cell_scan(f, dp, stream);
         launch_scatter_pairs(f, stream);
         launch_cell_sort(f, num_sms, stream);
-        launch_split(f, dp, max_occ, stream);
+        launch_split(f, dp, max_occ, num_sms, stream);
     }
     void enqueue_density(int b) {
         launch_density(frame_physics(b), dp, num_sms, shape, stream);
