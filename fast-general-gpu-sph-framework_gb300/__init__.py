@@ -48,6 +48,8 @@ FIELD_BLOCK_REQ = 9
 FIELD_COMPACT_INDEX = 10
 FIELD_TASKS = 11
 FIELD_SPLIT = 12
+FIELD_COLOR = 13
+FIELD_FINAL_POSITION = 14
 
 
 class GsphError(RuntimeError):
@@ -207,6 +209,7 @@ _SIGS = {
     "gsph_copy_out_async": ([_VP, C.c_int, _VP, C.c_size_t], C.c_int),
     "gsph_checksum": ([_VP, C.POINTER(C.c_double)], C.c_int),
     "gsph_tuning_default": ([C.POINTER(Tuning)], C.c_int),
+    "gsph_set_render_transform": ([_VP, C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int),
     "gsph_get_tuning": ([_VP, C.POINTER(Tuning)], C.c_int),
     "gsph_set_tuning": ([_VP, C.POINTER(Tuning)], C.c_int),
     "gsph_autotune": ([_VP, C.c_int, C.POINTER(Tuning), C.c_int, C.POINTER(Tuning),
@@ -408,9 +411,10 @@ class HybridSystem:
     def copy_out(self, field: int) -> np.ndarray:
         numc = self.params.numc
         n = self.n
-        if field in (FIELD_POSITION, FIELD_VELOCITY, FIELD_EVAL_VELOCITY, FIELD_ACCELERATION):
+        if field in (FIELD_POSITION, FIELD_VELOCITY, FIELD_EVAL_VELOCITY, FIELD_ACCELERATION,
+                     FIELD_FINAL_POSITION):
             out = np.empty((n, 4), np.float32)
-        elif field == FIELD_KEY:
+        elif field in (FIELD_KEY, FIELD_COLOR):
             out = np.empty(n, np.uint32)
         elif field in (FIELD_PERMUTATION, FIELD_COMPACT_INDEX):
             out = np.empty(n, np.int32)
@@ -446,6 +450,12 @@ class HybridSystem:
         _check(self._lib.gsph_reductions(self._h, out))
         keys = ("mass", "px", "py", "pz", "kinetic", "sx", "sy", "sz")
         return dict(zip(keys, out))
+
+    def set_render_transform(self, ratio=(1.0, 1.0, 1.0), origin=(0.0, 0.0, 0.0)) -> None:
+        """gsph_set_render_transform: FIELD_FINAL_POSITION = pos * ratio + origin."""
+        r = (C.c_float * 3)(*ratio)
+        o = (C.c_float * 3)(*origin)
+        _check(self._lib.gsph_set_render_transform(self._h, r, o))
 
     def get_tuning(self) -> Tuning:
         t = Tuning()

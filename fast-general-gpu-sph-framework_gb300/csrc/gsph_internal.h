@@ -182,6 +182,11 @@ void launch_density(const Frame &f, const DevParams &P, int num_sms,
 void launch_force(const Frame &f, const DevParams &P, int num_sms, bool fresh,
                   const LaunchShape &shape, cudaStream_t s);
 void launch_integrate(const Frame &f, const DevParams &P, cudaStream_t s);
+// Render-side buffers (headless): packed RGBA colour per particle from its
+// density and its path (TRA, paired SMS, single SMS), and render-space
+// positions.
+void launch_render(const Frame &f, float3 ratio, float3 origin, uint32_t *color,
+                   float4 *final_pos, cudaStream_t s);
 void launch_reductions(const float4 *pos, const float4 *vel, int n,
                        float mass, double *out8, cudaStream_t s);
 void launch_checksum(const float4 *pos, int n, double *out5, cudaStream_t s);

@@ -22,6 +22,8 @@
 // contiguous index range, pruned by micro-x slab as in the reference; the
 // interacting neighbours are visited in the same order (rows z-major, then
 // increasing sorted index), so sums match the reference's summation order.
+#include <algorithm>
+
 #include "gsph_internal.h"
 
 namespace gsph {
@@ -736,6 +738,53 @@ k_integrate(Frame f, DevParams P) {
     f.ev[i] = eo;
 }
 
+// ---------------------------------------------------------------- render --
+// COLORA (kernel_common.cuh:58): a * 255 << 24 | b << 16 | g << 8 | r, each
+// channel clamped to [0, 255] (the device conversion of the reference
+// saturates the same way).
+__device__ __forceinline__ uint32_t colora(float r, float g, float b, float a) {
+    auto ch = [](float v) { return uint32_t(fminf(fmaxf(v * 255.0f, 0.f), 255.f)); };
+    return (ch(a) << 24) | (ch(b) << 16) | (ch(g) << 8) | ch(r);
+}
+
+__device__ __forceinline__ float density_color(const Frame &f, int i) {
+    return (5000.f - 1.0f / f.pos[i].w) / 6000.f;
+}
+
+__global__ void __launch_bounds__(256)
+k_render_tra(Frame f, uint32_t *color) {
+    const int middle = f.ctr->middle;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < middle;
+         k += gridDim.x * blockDim.x) {
+        const int i = f.compact[k];
+        const float c = density_color(f, i);
+        color[i] = colora(c, 0.f, c, 1.f);
+    }
+}
+
+__global__ void __launch_bounds__(256)
+k_render_sms(Frame f, uint32_t *color) {
+    const int tasks = f.ctr->task_count;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < tasks * kSmsTaskParticles;
+         k += gridDim.x * blockDim.x) {
+        const gsph_block_task t = f.tasks[k / kSmsTaskParticles];
+        const int i = t.cell_begin + t.p_offset + k % kSmsTaskParticles;
+        if (i >= t.cell_begin + t.cell_particle_count) continue;
+        const float c = density_color(f, i);
+        color[i] = t.is_same ? colora(0.f, c, c, 1.f) : colora(c, c, 0.f, 1.f);
+    }
+}
+
+__global__ void __launch_bounds__(256)
+k_final_position(Frame f, float3 ratio, float3 origin, float4 *out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < f.n;
+         i += gridDim.x * blockDim.x) {
+        const float4 p = f.pos[i];
+        out[i] = make_float4(p.x * ratio.x + origin.x, p.y * ratio.y + origin.y,
+                             p.z * ratio.z + origin.z, 1.f);
+    }
+}
+
 // ------------------------------------------------------- FP64 reductions --
 // Deterministic two-level tree: fixed per-block partials, then one block.
 constexpr int kRedThreads = 256;
@@ -838,6 +887,17 @@ void launch_checksum(const float4 *pos, int n, double *out5, cudaStream_t s) {
 }
 
 // out8 must hold 8 + 8*kRedBlocks doubles.
+void launch_render(const Frame &f, float3 ratio, float3 origin, uint32_t *color,
+                   float4 *final_pos, cudaStream_t s) {
+    if (f.n <= 0) return;
+    const int blocks = std::min((f.n + 255) / 256, 4096);
+    if (color) {
+        k_render_tra<<<blocks, 256, 0, s>>>(f, color);
+        k_render_sms<<<blocks, 256, 0, s>>>(f, color);
+    }
+    if (final_pos) k_final_position<<<blocks, 256, 0, s>>>(f, ratio, origin, final_pos);
+}
+
 void launch_reductions(const float4 *pos, const float4 *vel, int n, float mass,
                        double *out8, cudaStream_t s) {
     k_reduce_partial<<<kRedBlocks, kRedThreads, 0, s>>>(pos, vel, n, mass,

@@ -102,6 +102,10 @@ struct System {
     uint64_t frames = 0;
 
     LaunchShape shape = kMaxShape;   // CTAs per SM of the density/force kernels
+    float3 render_ratio = make_float3(1.f, 1.f, 1.f);
+    float3 render_origin = make_float3(0.f, 0.f, 0.f);
+    uint32_t *render_color = nullptr;    // allocated on first use
+    float4 *render_pos = nullptr;
     int graph_frames = 0;   // frames per captured CUDA graph (0: stream launches)
     cudaGraphExec_t graph[2] = {nullptr, nullptr};   // by starting parity
 
@@ -805,6 +809,8 @@ size_t field_bytes(const System &s, gsph_field f, gsph_status &st) {
         case GSPH_FIELD_BLOCK_REQ: return size_t(s.numc) * 4;
         case GSPH_FIELD_MICRO_START: return (size_t(s.numc) * 64 + 1) * 4;
         case GSPH_FIELD_SPLIT: return 8;
+        case GSPH_FIELD_COLOR: return N * 4;
+        case GSPH_FIELD_FINAL_POSITION: return N * sizeof(float4);
         case GSPH_FIELD_TASKS: return 0;   // variable, checked separately
     }
     st = GSPH_ERR_INVALID_ARG;
@@ -1225,6 +1231,31 @@ gsph_status gsph_copy_out(gsph_handle h, gsph_field field, void *host_dst,
             o[1] = T;
             return GSPH_OK;
         }
+        case GSPH_FIELD_COLOR:
+        case GSPH_FIELD_FINAL_POSITION: {
+            if (!need) return GSPH_OK;
+            const bool color = field == GSPH_FIELD_COLOR;
+            if (color && !s.arranged) {
+                set_error("gsph_copy_out(COLOR): no arranged frame yet");
+                return GSPH_ERR_STATE;
+            }
+            if (color && !s.render_color &&
+                (st = s.alloc_n(&s.render_color, size_t(s.n_cap))))
+                return st;
+            if (!color && !s.render_pos && (st = s.alloc_n(&s.render_pos, size_t(s.n_cap))))
+                return st;
+            Frame f = s.fr;
+            f.pos = s.pos[s.cur];
+            launch_render(f, s.render_ratio, s.render_origin,
+                          color ? s.render_color : nullptr,
+                          color ? nullptr : s.render_pos, s.stream);
+            GSPH_CUDA(cudaGetLastError());
+            GSPH_CUDA(cudaStreamSynchronize(s.stream));
+            GSPH_CUDA(cudaMemcpy(host_dst, color ? static_cast<void *>(s.render_color)
+                                                 : static_cast<void *>(s.render_pos),
+                                 need, cudaMemcpyDeviceToHost));
+            return GSPH_OK;
+        }
         default: break;
     }
     set_error("gsph_copy_out: unsupported field %d", int(field));
@@ -1408,6 +1439,17 @@ gsph_status gsph_snapshot_load(const char *path, int device, gsph_handle *out) {
     }
     s.frames = frames;
     *out = h;
+    return GSPH_OK;
+}
+
+gsph_status gsph_set_render_transform(gsph_handle h, const float ratio[3],
+                                      const float origin[3]) {
+    if (!h || !ratio || !origin) {
+        set_error("gsph_set_render_transform: null argument");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    h->sys.render_ratio = make_float3(ratio[0], ratio[1], ratio[2]);
+    h->sys.render_origin = make_float3(origin[0], origin[1], origin[2]);
     return GSPH_OK;
 }
 

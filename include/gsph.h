@@ -171,7 +171,15 @@ typedef enum {
     GSPH_FIELD_BLOCK_REQ = 9,     /* int32[numc] SMS tasks per cell          */
     GSPH_FIELD_COMPACT_INDEX = 10,/* int32[N] TRA particles then SMS ones    */
     GSPH_FIELD_TASKS = 11,        /* gsph_block_task[T + (T&1)]              */
-    GSPH_FIELD_SPLIT = 12         /* int32[2] {middle, task count}           */
+    GSPH_FIELD_SPLIT = 12,        /* int32[2] {middle, task count}           */
+    /* Headless render-side buffers, computed on demand from the current state
+     * and the last arrange (the reference writes them every frame for its GL
+     * view, density_kernels.cu:361-365,547-562, integration_kernels.cu:331-335;
+     * its headless build leaves them out): */
+    GSPH_FIELD_COLOR = 13,        /* uint32[N] RGBA8, COLORA of (5000-rho)/6000:
+                                     TRA (c,0,c), paired SMS (0,c,c), single
+                                     SMS (c,c,0)                              */
+    GSPH_FIELD_FINAL_POSITION = 14 /* float4[N] position * ratio + origin, w=1 */
 } gsph_field;
 
 const char *gsph_last_error(void);
@@ -289,6 +297,12 @@ gsph_status gsph_copy_in_async(gsph_handle h, gsph_field field,
                                const void *host_src, size_t bytes);
 gsph_status gsph_copy_out_async(gsph_handle h, gsph_field field,
                                 void *host_dst, size_t bytes);
+
+/* Render-space transform of GSPH_FIELD_FINAL_POSITION (the reference's
+ * sim_ratio / sim_origin, sph_hybrid_system.cpp:221-224); default ratio 1,
+ * origin 0. */
+gsph_status gsph_set_render_transform(gsph_handle h, const float ratio[3],
+                                      const float origin[3]);
 
 /* Split thresholds and launch shapes (see gsph_tuning). */
 gsph_status gsph_tuning_default(gsph_tuning *out);

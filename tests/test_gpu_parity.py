@@ -326,3 +326,36 @@ def test_step_equals_stage_sequence(gsph, scene):
         with pytest.raises(gsph.GsphError) as ei:
             b.density()                     # positions moved since the arrange
         assert ei.value.status == gsph.ERR_STATE
+
+
+def test_render_buffers(gsph, cuda_device):
+    """Headless colour and render-space positions (the reference's GUI
+    buffers): colour from each particle's density and path, positions
+    scaled and shifted."""
+    _, p, pos = dense_scene(gsph, n_side=14)
+    with make(gsph, p, shuffled(pos)) as s:
+        s.step(2)
+        s.set_render_transform((2.0, 0.5, 1.0), (1.0, -1.0, 0.25))
+        fp = s.copy_out(gsph.FIELD_FINAL_POSITION)
+        sp = s.copy_out(gsph.FIELD_POSITION)
+        col = s.copy_out(gsph.FIELD_COLOR)
+        compact = s.copy_out(gsph.FIELD_COMPACT_INDEX)
+        split = s.copy_out(gsph.FIELD_SPLIT)
+        tasks = s.copy_out(gsph.FIELD_TASKS)
+    want = sp[:, :3] * np.array([2.0, 0.5, 1.0], np.float32) + np.array([1.0, -1.0, 0.25],
+                                                                        np.float32)
+    assert np.allclose(fp[:, :3], want, rtol=1e-6, atol=1e-6) and np.all(fp[:, 3] == 1.0)
+    c = np.clip((5000.0 - 1.0 / sp[:, 3].astype(np.float64)) / 6000.0 * 255.0, 0, 255)
+    c = c.astype(np.uint32)
+    r, g, b, a = col & 255, (col >> 8) & 255, (col >> 16) & 255, col >> 24
+    assert np.all(a == 255)
+    tra = compact[: split[0]]
+    assert np.all(np.abs(r[tra].astype(int) - c[tra]) <= 1) and np.all(g[tra] == 0)
+    for t in tasks[: split[1]]:
+        idx = np.arange(t["cell_begin"] + t["p_offset"],
+                        min(t["cell_begin"] + t["p_offset"] + 32,
+                            t["cell_begin"] + t["cell_particle_count"]))
+        if t["is_same"]:
+            assert np.all(r[idx] == 0) and np.all(np.abs(g[idx].astype(int) - c[idx]) <= 1)
+        else:
+            assert np.all(b[idx] == 0) and np.all(np.abs(r[idx].astype(int) - c[idx]) <= 1)
