@@ -211,18 +211,27 @@ k_cell_scan_apply(const int32_t *__restrict__ count, int numc,
     unsigned long long wprefix = 0;
     for (int w = 0; w < warp; ++w) wprefix += ws[w];
     unsigned long long run = tiles[blockIdx.x] + wprefix + x - s;
+    int out[kScanItems];
 #pragma unroll
     for (int q = 0; q < kScanItems; ++q) {
         const int c = first + q;
-        if (c < numc) {
-            cell_start[c] = int32_t(run & 0xFFFFFFFFull);
-            if (v[q] > 0) {
-                occ_list[run >> 32] = c;
-                if (v[q] > kSmallCellMax)
-                    big_list[atomicAdd(&ctr->num_big, 1)] = c;
-            }
+        out[q] = int32_t(run & 0xFFFFFFFFull);
+        if (c < numc && v[q] > 0) {
+            occ_list[run >> 32] = c;
+            if (v[q] > kSmallCellMax) big_list[atomicAdd(&ctr->num_big, 1)] = c;
         }
         run += pack_cell(v[q]);
+    }
+    if (first + kScanItems <= numc) {
+        // a thread's cells are contiguous: 16-byte stores
+        int4 *dst = reinterpret_cast<int4 *>(cell_start + first);
+#pragma unroll
+        for (int q = 0; q < kScanItems / 4; ++q)
+            dst[q] = make_int4(out[4 * q], out[4 * q + 1], out[4 * q + 2], out[4 * q + 3]);
+    } else {
+#pragma unroll
+        for (int q = 0; q < kScanItems; ++q)
+            if (first + q < numc) cell_start[first + q] = out[q];
     }
 }
 
