@@ -22,6 +22,8 @@
 //   * per cell, the three micro-x slab boundaries are kept (10 bits each) in
 //     place of the dense micro table; stale entries of empty cells are harmless
 //     because every use clamps them by the cell's count.
+#include <algorithm>
+
 #include "gsph_internal.h"
 
 namespace gsph {
@@ -30,40 +32,7 @@ namespace {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
 
-__device__ __forceinline__ unsigned lanemask_lt() {
-    unsigned m;
-    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-    return m;
-}
 
-// Micro key of one position (sph_utils.cuh:44-99), in the global cell space
-// of a batch: the scene's cell base is added to the reference's cell index.
-// Positions outside the scene's grid raise kErrOutOfDomain and are clamped to
-// the nearest cell so that no index ever leaves the tables.
-__device__ __forceinline__ uint32_t micro_key(float4 p, const DevParams &P,
-                                              const SceneGeom &G,
-                                              Counters *ctr, int i) {
-    const float fx = floorf(p.x * P.rat);
-    const float fy = floorf(p.y * P.rat);
-    const float fz = floorf(p.z * P.rat);
-    const float lx = float(G.gx << 2), ly = float(G.gy << 2),
-                lz = float(G.gz << 2);
-    int mx, my, mz;
-    if (fx >= 0.f && fx < lx && fy >= 0.f && fy < ly && fz >= 0.f && fz < lz) {
-        mx = int(fx);
-        my = int(fy);
-        mz = int(fz);
-    } else {
-        mx = (fx >= 0.f) ? min(int(fminf(fx, lx - 1.f)), (G.gx << 2) - 1) : 0;
-        my = (fy >= 0.f) ? min(int(fminf(fy, ly - 1.f)), (G.gy << 2) - 1) : 0;
-        mz = (fz >= 0.f) ? min(int(fminf(fz, lz - 1.f)), (G.gz << 2) - 1) : 0;
-        if (atomicOr(&ctr->err, kErrOutOfDomain) == 0u) ctr->err_index = i;
-    }
-    const uint32_t c = uint32_t(G.cbase) + uint32_t(mx >> 2) +
-                       uint32_t(G.gx) * (uint32_t(my >> 2) + uint32_t(G.gy) * uint32_t(mz >> 2));
-    const uint32_t sub = uint32_t(my & 3) | (uint32_t(mz & 3) << 2) | (uint32_t(mx & 3) << 4);
-    return (c << 6) | sub;
-}
 
 // ---------------------------------------------------------------------------
 // A2: key + per-coarse-cell slot (warp-aggregated atomics).
@@ -77,15 +46,34 @@ k_hash_count(const float4 *__restrict__ pos, int n, DevParams P, SceneTable T,
     if (!valid) return;
     const SceneGeom G = geom_of_particle(T, i);
     const uint32_t key = micro_key(pos[i], P, G, ctr, i);
-    const uint32_t cell = key >> 6;
-    const unsigned peers = __match_any_sync(active, cell);
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(peers) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(&cell_count[cell], __popc(peers));
-    base = __shfl_sync(peers, base, leader);
     key_out[i] = key;
-    slot_out[i] = uint32_t(base + __popc(peers & lanemask_lt()));
+    slot_out[i] = cell_slot(cell_count, key >> 6, active);
+}
+
+// The particles the previous split sent to SMS tasks (compact[middle, n)),
+// whose keys the force pass did not compute ahead.
+__global__ void __launch_bounds__(256)
+k_hash_sms(const float4 *__restrict__ pos, int n, DevParams P, SceneTable T,
+           const int32_t *__restrict__ compact, uint32_t *__restrict__ key_out,
+           uint32_t *__restrict__ slot_out, int32_t *__restrict__ cell_count,
+           Counters *ctr) {
+    const int middle = ctr->middle;
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    // warp-uniform loop: every lane of a warp sees the same base
+    for (int base = middle + warp * 32; base < n; base += warps * 32) {
+        const int k = base + lane;
+        const bool valid = k < n;
+        const unsigned active = __ballot_sync(kFull, valid);
+        if (valid) {
+            const int i = compact[k];
+            const SceneGeom G = geom_of_particle(T, i);
+            const uint32_t key = micro_key(pos[i], P, G, ctr, i);
+            key_out[i] = key;
+            slot_out[i] = cell_slot(cell_count, key >> 6, active);
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -354,6 +342,12 @@ __global__ void __launch_bounds__(256) k_sort_big(Frame f) {
 }
 
 }  // namespace
+
+void launch_hash_sms(const Frame &f, const DevParams &P, cudaStream_t s) {
+    if (f.n <= 0) return;
+    k_hash_sms<<<std::min((f.n + 255) / 256, 4096), 256, 0, s>>>(
+        f.pos_in, f.n, P, f.scenes, f.compact, f.key_in, f.slot, f.cell_count, f.ctr);
+}
 
 void launch_hash_count(const Frame &f, const DevParams &P, cudaStream_t s) {
     if (f.n <= 0) return;

@@ -132,6 +132,11 @@ struct Frame {
     // advance) and writes the new state here instead of leaving it to a
     // separate integration launch; the arrays must not alias pos/vel/ev.
     float4 *pos_next, *vel_next, *ev_next;
+    // With pos_next set and hash_next true, the TRA force pass also computes
+    // the next frame's micro key and cell slot of its particles (key_in, slot,
+    // cell_count); the SMS particles are hashed at the start of the next
+    // arrange (launch_hash_sms), before the split overwrites the compact list.
+    bool hash_next;
     uint32_t *key_in, *slot;                   // per source particle
     unsigned long long *pairs;                 // (key << 32 | src), by cell
     uint32_t *key;                             // sorted keys
@@ -160,8 +165,61 @@ struct Frame {
     Counters *ctr;
 };
 
+// ---- shared device helpers (grid sort and the force pass's look-ahead hash) ----
+#ifdef __CUDACC__
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Micro key of one position (sph_utils.cuh:44-99), in the global cell space
+// of a batch: the scene's cell base is added to the reference's cell index.
+// Positions outside the scene's grid raise kErrOutOfDomain and are clamped to
+// the nearest cell so that no index ever leaves the tables.
+__device__ __forceinline__ uint32_t micro_key(float4 p, const DevParams &P,
+                                              const SceneGeom &G,
+                                              Counters *ctr, int i) {
+    const float fx = floorf(p.x * P.rat);
+    const float fy = floorf(p.y * P.rat);
+    const float fz = floorf(p.z * P.rat);
+    const float lx = float(G.gx << 2), ly = float(G.gy << 2),
+                lz = float(G.gz << 2);
+    int mx, my, mz;
+    if (fx >= 0.f && fx < lx && fy >= 0.f && fy < ly && fz >= 0.f && fz < lz) {
+        mx = int(fx);
+        my = int(fy);
+        mz = int(fz);
+    } else {
+        mx = (fx >= 0.f) ? min(int(fminf(fx, lx - 1.f)), (G.gx << 2) - 1) : 0;
+        my = (fy >= 0.f) ? min(int(fminf(fy, ly - 1.f)), (G.gy << 2) - 1) : 0;
+        mz = (fz >= 0.f) ? min(int(fminf(fz, lz - 1.f)), (G.gz << 2) - 1) : 0;
+        if (atomicOr(&ctr->err, kErrOutOfDomain) == 0u) ctr->err_index = i;
+    }
+    const uint32_t c = uint32_t(G.cbase) + uint32_t(mx >> 2) +
+                       uint32_t(G.gx) * (uint32_t(my >> 2) + uint32_t(G.gy) * uint32_t(mz >> 2));
+    const uint32_t sub = uint32_t(my & 3) | (uint32_t(mz & 3) << 2) | (uint32_t(mx & 3) << 4);
+    return (c << 6) | sub;
+}
+
+// Slot of a particle among its cell's particles: one atomic per cell per warp
+// (lanes in `active` with the same cell share it, match.any).
+__device__ __forceinline__ uint32_t cell_slot(int32_t *cell_count, uint32_t cell,
+                                              unsigned active) {
+    const unsigned peers = __match_any_sync(active, cell);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(&cell_count[cell], __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    return uint32_t(base + __popc(peers & lanemask_lt()));
+}
+#endif  // __CUDACC__
+
 // ---- launchers (grid.cu) ----
 void launch_hash_count(const Frame &f, const DevParams &P, cudaStream_t s);
+// Hash of the previous split's SMS particles only (compact[middle, n)).
+void launch_hash_sms(const Frame &f, const DevParams &P, cudaStream_t s);
 void launch_cell_scan(const Frame &f, const DevParams &P, cudaStream_t s);
 void launch_scatter_pairs(const Frame &f, cudaStream_t s);
 void launch_cell_sort(const Frame &f, int num_sms, cudaStream_t s);

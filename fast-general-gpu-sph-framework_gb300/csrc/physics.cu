@@ -252,6 +252,11 @@ __device__ __forceinline__ void write_force(const Frame &f, const DevParams &P,
         f.pos_next[self] = po;
         f.vel_next[self] = vo;
         f.ev_next[self] = eo;
+        if (f.hash_next && !sms) {   // SMS particles: k_hash_sms next frame
+            const uint32_t key = micro_key(po, P, G, f.ctr, self);
+            f.key_in[self] = key;
+            f.slot[self] = cell_slot(f.cell_count, key >> 6, __activemask());
+        }
     }
 }
 
@@ -456,6 +461,7 @@ k_density_sms(Frame f, DevParams P) {
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int task_count = f.ctr->task_count;
+    if (task_count == 0) return;   // no SMS work: skip the queue atomics
     float *sx = sms_x[warp], *sy = sms_y[warp], *sz = sms_z[warp];
     for (;;) {
         const int u = next_unit(&f.ctr->work_density_sms);
@@ -516,6 +522,7 @@ k_force_tra(Frame f, DevParams P, bool fresh) {
     const int lane = threadIdx.x & 31;
     const int middle = f.ctr->middle;
     const int units = (middle + 31) >> 5;
+    if (units == 0) return;        // no TRA work: skip the queue atomics
     for (;;) {
         const int u = next_unit(&f.ctr->work_force);
         if (u >= units) break;
@@ -611,6 +618,7 @@ k_force_sms(Frame f, DevParams P) {
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int task_count = f.ctr->task_count;
+    if (task_count == 0) return;   // no SMS work: skip the queue atomics
     float *sx = sm[0][warp], *sy = sm[1][warp], *sz = sm[2][warp], *sw = sm[3][warp];
     float *svx = sm[4][warp], *svy = sm[5][warp], *svz = sm[6][warp], *spr = sm[7][warp];
     for (;;) {

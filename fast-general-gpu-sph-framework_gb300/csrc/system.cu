@@ -99,6 +99,15 @@ struct System {
     bool arranged = false;   // sorted state + split valid
     bool grid_current = false;   // no position changed since the last arrange
     bool lists_valid = false;   // TRA neighbour masks match the state
+    // hashed: key_in / slot / cell_count hold the micro keys and cell slots
+    // of the current state (computed ahead by the last frame's force pass),
+    // so the next arrange skips its hash launch. counts_dirty: cell_count may
+    // hold counts that no arrange will consume (cleared before a new hash).
+    bool hashed = false;
+    bool counts_dirty = false;
+    // sms_pending: the hash ahead covered the TRA particles only; the previous
+    // split's SMS particles still need theirs (launch_hash_sms).
+    bool sms_pending = false;
     uint64_t frames = 0;
 
     LaunchShape shape = kMaxShape;   // CTAs per SM of the density/force kernels
@@ -422,6 +431,8 @@ struct System {
         arranged = false;
         grid_current = false;
         lists_valid = false;
+        hashed = false;
+        counts_dirty = true;
         GSPH_CUDA(cudaStreamSynchronize(stream));
         return GSPH_OK;
     }
@@ -449,14 +460,35 @@ struct System {
         return f;
     }
 
+    // Hash of the current state into key_in / slot / cell_count.
+    void enqueue_hash(int in) {
+        if (counts_dirty)
+            cudaMemsetAsync(fr.cell_count, 0, sizeof(int32_t) * size_t(c_cap), stream);
+        launch_hash_count(frame_arrange(in), dp, stream);
+        hashed = true;
+        sms_pending = false;
+        counts_dirty = true;
+    }
+    // Completes a TRA-only hash ahead with the previous split's SMS particles.
+    void enqueue_hash_sms(int in) {
+        launch_hash_sms(frame_arrange(in), dp, stream);
+        sms_pending = false;
+    }
+
     void enqueue_arrange(int in) {
         lists_valid = false;
         const Frame f = frame_arrange(in);
-        launch_hash_count(f, dp, stream);
+        if (!hashed)
+            enqueue_hash(in);
+        else if (sms_pending)
+            enqueue_hash_sms(in);
         launch_cell_scan(f, dp, stream);
         launch_scatter_pairs(f, stream);
         launch_cell_sort(f, num_sms, stream);
         launch_split(f, dp, max_occ, num_sms, stream);
+        hashed = false;          // consumed; the sort cleared the counts
+        sms_pending = false;
+        counts_dirty = false;
     }
     void enqueue_density(int b) {
         launch_density(frame_physics(b), dp, num_sms, shape, stream);
@@ -473,12 +505,17 @@ struct System {
         f.pos_next = pos[1 - b];
         f.vel_next = vel[1 - b];
         f.ev_next = ev[1 - b];
+        f.hash_next = true;
         launch_force(f, dp, num_sms, lists_valid, shape, stream);
         lists_valid = false;
+        hashed = true;
+        sms_pending = true;
+        counts_dirty = true;
     }
     void enqueue_advance(int b) {
         launch_integrate(frame_physics(b), dp, stream);
         lists_valid = false;
+        hashed = false;
     }
 
     gsph_status check_launch() {
@@ -505,6 +542,9 @@ struct System {
     gsph_status build_graph(int parity) {
         cudaGraph_t g = nullptr;
         GSPH_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        // graph launches are preceded by a complete hash of the state
+        hashed = true;
+        sms_pending = false;
         for (int k = 0; k < graph_frames; ++k) {
             enqueue_arrange(parity);
             enqueue_density(1 - parity);
@@ -570,12 +610,20 @@ struct System {
     gsph_status step(int n) {
         if (numc == 0) return GSPH_OK;   // a batch without scenes
         if (graph_frames > 0 && !timing) {
+            // captured frames start from a hashed state and leave one behind
+            if (n >= graph_frames && !hashed) enqueue_hash(cur);
+            if (n >= graph_frames && sms_pending) enqueue_hash_sms(cur);
+            GSPH_CUDA(cudaGetLastError());
             while (n >= graph_frames) {
                 if (!graph[cur]) {
                     gsph_status st = build_graph(cur);
                     if (st) return st;
                 }
                 GSPH_CUDA(cudaGraphLaunch(graph[cur], stream));
+                hashed = true;
+                counts_dirty = true;
+                if (n - graph_frames >= graph_frames) enqueue_hash_sms(cur);
+                else sms_pending = true;
                 arranged = true;
                 grid_current = false;
                 lists_valid = false;
@@ -738,6 +786,8 @@ struct System {
         arranged = arranged0;
         grid_current = grid0;
         lists_valid = false;
+        hashed = false;
+        counts_dirty = true;
         graph_frames = graphs0;
         timing = timing0;
         cudaStreamSynchronize(stream);
@@ -1342,7 +1392,10 @@ gsph_status gsph_copy_in(gsph_handle h, gsph_field field, const void *host_src,
     if (bytes) GSPH_CUDA(cudaMemcpy(dst, host_src, bytes, cudaMemcpyHostToDevice));
     s.lists_valid = false;   // the masks describe the old state
     // new positions need a new grid (cell lists and the sorted x/y/z copy)
-    if (field == GSPH_FIELD_POSITION) s.grid_current = false;
+    if (field == GSPH_FIELD_POSITION) {
+        s.grid_current = false;
+        s.hashed = false;
+    }
     return GSPH_OK;
 }
 
@@ -1360,7 +1413,10 @@ gsph_status gsph_copy_in_async(gsph_handle h, gsph_field field,
         GSPH_CUDA(cudaMemcpyAsync(dst, host_src, bytes, cudaMemcpyHostToDevice,
                                   s.stream));
     s.lists_valid = false;   // the masks describe the old state
-    if (field == GSPH_FIELD_POSITION) s.grid_current = false;
+    if (field == GSPH_FIELD_POSITION) {
+        s.grid_current = false;
+        s.hashed = false;
+    }
     return GSPH_OK;
 }
 
