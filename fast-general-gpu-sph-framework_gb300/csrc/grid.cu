@@ -170,6 +170,7 @@ k_cell_scan_tiles(unsigned long long *__restrict__ tiles, int ntiles,
         ctr->work_force = 0;
         ctr->work_density_sms = 0;
         ctr->work_force_sms = 0;
+        ctr->any_sms = 0;
     }
 }
 

@@ -119,7 +119,11 @@ struct Counters {
     int32_t err_index;      // first offending particle (best effort)
     int32_t work_density_sms;   //   SMS tasks of density / force
     int32_t work_force_sms;
-    int32_t pad[21];
+    // Set when some cell takes the SMS path this frame; when clear, every
+    // particle is TRA, the compact index is the identity and the TRA/SMS
+    // compaction is skipped.
+    int32_t any_sms;
+    int32_t pad[20];
 };
 
 // Per-frame device pointers of one batch of scenes.

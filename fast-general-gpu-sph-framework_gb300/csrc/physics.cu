@@ -296,12 +296,13 @@ k_density_tra(Frame f, DevParams P) {
     const int lane = threadIdx.x & 31;
     const int middle = f.ctr->middle;
     const int units = (middle + 31) >> 5;
+    const bool ident = !f.ctr->any_sms;   // all TRA: compact is the identity
     for (;;) {
         const int u = next_unit(&f.ctr->work_density);
         if (u >= units) break;
         const int idx = (u << 5) + lane;
         if (idx >= middle) continue;
-        const int self = f.compact[idx];
+        const int self = ident ? idx : f.compact[idx];
         const float4 p = f.pos[self];
         const SceneGeom G = geom_of_particle(f.scenes, self);
         const MicroPos mp = micro_of(p, P, G);
@@ -522,13 +523,14 @@ k_force_tra(Frame f, DevParams P, bool fresh) {
     const int lane = threadIdx.x & 31;
     const int middle = f.ctr->middle;
     const int units = (middle + 31) >> 5;
+    const bool ident = !f.ctr->any_sms;   // all TRA: compact is the identity
     if (units == 0) return;        // no TRA work: skip the queue atomics
     for (;;) {
         const int u = next_unit(&f.ctr->work_force);
         if (u >= units) break;
         const int idx = (u << 5) + lane;
         if (idx >= middle) continue;
-        const int self = f.compact[idx];
+        const int self = ident ? idx : f.compact[idx];
         const float4 p = f.pos[self];
         const float4 pev = f.ev[self];
         const SceneGeom G = geom_of_particle(f.scenes, self);
@@ -764,7 +766,7 @@ k_render_tra(Frame f, uint32_t *color) {
     const int middle = f.ctr->middle;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < middle;
          k += gridDim.x * blockDim.x) {
-        const int i = f.compact[k];
+        const int i = f.ctr->any_sms ? f.compact[k] : k;
         const float c = density_color(f, i);
         color[i] = colora(c, 0.f, c, 1.f);
     }

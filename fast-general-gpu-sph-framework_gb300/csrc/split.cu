@@ -33,10 +33,11 @@ __device__ __forceinline__ int cell_n(const int32_t *__restrict__ start, int c) 
 // A6: SMS task count of one cell (gpu_model.cu:137-181, same neighbour
 // bounds tests; the thresholds are the reference's unless tuned).
 __global__ void __launch_bounds__(256)
-k_cell_model(const int32_t *__restrict__ occ, const Counters *ctr,
+k_cell_model(const int32_t *__restrict__ occ, Counters *ctr,
              const int32_t *__restrict__ start, SceneTable T, int3 thr,
              int4 *__restrict__ val) {
     const int num_occ = ctr->num_occ;
+    bool any = false;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < num_occ;
          k += gridDim.x * blockDim.x) {
     const int gidx = occ[k];
@@ -64,7 +65,9 @@ k_cell_model(const int32_t *__restrict__ occ, const Counters *ctr,
         req = (self + 31) >> 5;
     const int sms = min(req * kSmsTaskParticles, self);
     val[k] = make_int4(req, sms, self - sms, 0);
+    any |= req > 0;
     }
+    if (__any_sync(kFull, any) && (threadIdx.x & 31) == 0) atomicOr(&ctr->any_sms, 1);
 }
 
 __device__ __forceinline__ int4 add4(int4 a, int4 b) {
@@ -85,6 +88,7 @@ __device__ __forceinline__ int4 shfl_down4(int4 v, int o) {
 __global__ void __launch_bounds__(kScanThreads)
 k_val_scan_reduce(const int4 *__restrict__ in, const Counters *ctr,
                   int4 *__restrict__ tiles) {
+    if (!ctr->any_sms) return;   // all TRA: nothing to compact
     const int n = ctr->num_occ;
     __shared__ int4 ws[kScanThreads / 32];
     for (int tile = blockIdx.x; tile * kScanTile < n; tile += gridDim.x) {
@@ -107,7 +111,16 @@ k_val_scan_reduce(const int4 *__restrict__ in, const Counters *ctr,
 }
 
 __global__ void __launch_bounds__(1024)
-k_val_scan_tiles(int4 *__restrict__ tiles, Counters *ctr, int task_capacity) {
+k_val_scan_tiles(int4 *__restrict__ tiles, Counters *ctr, int task_capacity,
+                 int n_particles) {
+    if (!ctr->any_sms) {         // all TRA
+        if (threadIdx.x == 0) {
+            ctr->task_count = 0;
+            ctr->n_sms = 0;
+            ctr->middle = n_particles;
+        }
+        return;
+    }
     const int ntiles = (ctr->num_occ + kScanTile - 1) / kScanTile;
     __shared__ int4 ws[32];
     __shared__ int4 carry;
@@ -159,6 +172,7 @@ k_val_scan_tiles(int4 *__restrict__ tiles, Counters *ctr, int task_capacity) {
 __global__ void __launch_bounds__(kScanThreads)
 k_val_scan_apply(const int4 *__restrict__ in, const Counters *ctr,
                  const int4 *__restrict__ tiles, int4 *__restrict__ out) {
+    if (!ctr->any_sms) return;
     const int n = ctr->num_occ;
     __shared__ int4 ws[kScanThreads / 32];
     for (int tile = blockIdx.x; tile * kScanTile < n; tile += gridDim.x) {
@@ -206,6 +220,7 @@ k_cell_emit(const int32_t *__restrict__ occ, const Counters *ctr,
             const int4 *__restrict__ val, const int4 *__restrict__ prefix,
             SceneTable T, int32_t *__restrict__ compact,
             gsph_block_task *__restrict__ tasks) {
+    if (!ctr->any_sms) return;   // all TRA: the compact index is the identity
     const int num_occ = ctr->num_occ;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < num_occ;
          k += gridDim.x * blockDim.x) {
@@ -326,7 +341,7 @@ void launch_split(const Frame &f, const DevParams &P, int max_occ, int num_sms,
         make_int3(P.sparse_total, P.sparse_self, P.mid_total), f.cell_val);
     k_val_scan_reduce<<<ntiles, kScanThreads, 0, s>>>(f.cell_val, f.ctr,
                                                      f.scan_tiles4);
-    k_val_scan_tiles<<<1, 1024, 0, s>>>(f.scan_tiles4, f.ctr, f.task_capacity);
+    k_val_scan_tiles<<<1, 1024, 0, s>>>(f.scan_tiles4, f.ctr, f.task_capacity, f.n);
     k_val_scan_apply<<<ntiles, kScanThreads, 0, s>>>(f.cell_val, f.ctr,
                                                     f.scan_tiles4, f.cell_prefix);
     k_cell_emit<<<cap128, 128, 0, s>>>(

@@ -1234,6 +1234,11 @@ gsph_status gsph_copy_out(gsph_handle h, gsph_field field, void *host_dst,
             if (need) GSPH_CUDA(cudaMemcpy(host_dst, s.fr.perm, need, cudaMemcpyDeviceToHost));
             return GSPH_OK;
         case GSPH_FIELD_COMPACT_INDEX:
+            if (s.arranged && !c.any_sms) {   // all TRA: the identity, not stored
+                int32_t *o = static_cast<int32_t *>(host_dst);
+                for (int i = 0; i < s.n; ++i) o[i] = i;
+                return GSPH_OK;
+            }
             if (need) GSPH_CUDA(cudaMemcpy(host_dst, s.fr.compact, need, cudaMemcpyDeviceToHost));
             return GSPH_OK;
         case GSPH_FIELD_CELL_START:
