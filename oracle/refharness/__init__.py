@@ -2,7 +2,8 @@
 
 run_tick() runs one reference frame (arrange, density, force, integrate) on a
 given state with the reference's own kernels and returns every intermediate
-array; run_bench() runs the reference's benchmark loop and returns its report.
+array; run_frames() steps whole frames and returns the final state;
+run_bench() runs the reference's benchmark loop and returns its report.
 Both need a GPU and oracle/_ref/ (see build_ref.py).
 """
 from __future__ import annotations
@@ -71,6 +72,20 @@ def run_tick(params, pos4, vel4=None, ev4=None, timeout=600) -> dict:
         write_input(td / "in.bin", params, pos4, vel4, ev4)
         (td / "out").mkdir()
         subprocess.run([str(HARNESS), str(CUBIN), "tick", str(td / "in.bin"),
+                        str(td / "out")], check=True, timeout=timeout)
+        return _read_dir(td / "out")
+
+
+def run_frames(params, pos4, frames: int, timeout=1800) -> dict:
+    """final_pos (n, 4), final_vel (n, 3), final_ev (n, 4) after `frames`
+    reference frames from the given positions at rest."""
+    if not available():
+        raise RuntimeError("reference harness not built (oracle/_ref)")
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        write_input(td / "in.bin", params, pos4)
+        (td / "out").mkdir()
+        subprocess.run([str(HARNESS), str(CUBIN), "run", str(td / "in.bin"), str(frames),
                         str(td / "out")], check=True, timeout=timeout)
         return _read_dir(td / "out")
 

@@ -22,9 +22,11 @@
 // Usage:
 //   ref_harness <cubin> tick  <input.bin> <out_dir>
 //   ref_harness <cubin> bench <input.bin> <frames>
+//   ref_harness <cubin> run   <input.bin> <frames> <out_dir>
 // input.bin: "GSPHREF1", gsph_params, int32 n, float4 pos[n], float4 vel[n],
 // float4 ev[n]. tick writes raw arrays + meta.txt into out_dir; bench prints
-// one JSON line with the reference's benchmark fields.
+// one JSON line with the reference's benchmark fields; run steps whole frames
+// (tick) and writes the final position, velocity and evaluated velocity.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -516,18 +518,48 @@ static int run_bench(const Kernels &k, const Scene &sc, int frames) {
     return 0;
 }
 
+// `frames` whole reference frames (tick, sph_hybrid_system.cpp:253-339),
+// then the final state.
+static int run_frames(const Kernels &k, const Scene &sc, int frames,
+                      const std::string &dir) {
+    RefState st = make_state(sc, k);
+    const float inv_cell = sc.p.inv_cell_size;
+    FILE *meta = std::fopen((dir + "/meta.txt").c_str(), "w");
+    if (!meta) {
+        std::fprintf(stderr, "cannot write into %s\n", dir.c_str());
+        return 2;
+    }
+    for (int i = 0; i < frames; ++i) {
+        arrange(st, k, inv_cell);
+        physics(st, k, const_cast<CUfunction *>(k.density));
+        physics(st, k, const_cast<CUfunction *>(k.force));
+        advance(st, k);
+    }
+    CK(cudaDeviceSynchronize());
+    const size_t N = size_t(st.n);
+    std::fprintf(meta, "middle %d\ntask_count %d\n", st.middle, st.task_count);
+    dump<float>(dir, "final_pos", st.buf.position_d, N * 4, meta, "float32", 4);
+    dump<float>(dir, "final_vel", st.buf.velocity, N * 3, meta, "float32", 3);
+    dump<float>(dir, "final_ev", st.buf.evaluated_velocity, N * 4, meta, "float32", 4);
+    std::fclose(meta);
+    return 0;
+}
+
 int main(int argc, char **argv) {
     if (argc < 5) {
         std::fprintf(stderr,
                      "usage: %s <cubin> tick <input.bin> <out_dir>\n"
-                     "       %s <cubin> bench <input.bin> <frames>\n",
-                     argv[0], argv[0]);
+                     "       %s <cubin> bench <input.bin> <frames>\n"
+                     "       %s <cubin> run <input.bin> <frames> <out_dir>\n",
+                     argv[0], argv[0], argv[0]);
         return 2;
     }
     const Kernels k = load_kernels(argv[1]);
     const Scene sc = read_input(argv[3]);
     if (!std::strcmp(argv[2], "tick")) return run_tick(k, sc, argv[4]);
     if (!std::strcmp(argv[2], "bench")) return run_bench(k, sc, std::atoi(argv[4]));
+    if (!std::strcmp(argv[2], "run") && argc >= 6)
+        return run_frames(k, sc, std::atoi(argv[4]), argv[5]);
     std::fprintf(stderr, "unknown mode %s\n", argv[2]);
     return 2;
 }
