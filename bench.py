@@ -160,13 +160,15 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel: str):
-    """Per-launch DRAM bytes of `kernel` from the committed ncu summary."""
+def ncu_traffic(kernel: str, key: str = ""):
+    """Per-launch DRAM bytes of `kernel` (or its `.key` figure) from the
+    committed ncu summary."""
     f = ROOT / "profiles" / "traffic_per_launch.txt"
     if not f.exists():
         return None
+    name = re.escape(kernel + (f".{key}" if key else ""))
     for line in f.read_text().splitlines():
-        m = re.match(rf"\s*{kernel}\s*=\s*([0-9.eE+]+)", line)
+        m = re.match(rf"\s*{name}\s*=\s*([0-9.eE+]+)", line)
         if m:
             return float(m.group(1))
     return None
@@ -740,6 +742,7 @@ def measure_scene(g, sysm, args, ws, rank, local, dist, workload, cpu_state):
         "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "algorithmic_bytes": b_dom,
+                     "fp32_pipe_frac": ncu_traffic(kernel, "fma_pipe"),
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
                      if peak_kind == "measured" else "fallback 6800 GB/s"},
         "roofline_stages": per_stage,
