@@ -150,6 +150,23 @@ class Tuning(C.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved_"}
 
 
+class ServerConfig(C.Structure):
+    """gsph_server_config."""
+    _fields_ = [("budget_bytes", C.c_uint64), ("particle_capacity", C.c_uint64),
+                ("cell_capacity", C.c_uint64), ("scene_capacity", C.c_uint32),
+                ("chunk_frames", C.c_int32), ("device", C.c_int32), ("reserved_", C.c_int32)]
+
+
+class ServerStats(C.Structure):
+    """gsph_server_stats."""
+    _fields_ = [(n, C.c_uint64) for n in (
+        "submitted", "finished", "rejected", "frames", "chunks", "particle_steps",
+        "queued", "resident", "resident_particles", "resident_bytes")]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 class BenchReport(C.Structure):
     _fields_ = [
         ("measured_frames", C.c_int32), ("warmup_frames", C.c_int32),
@@ -209,6 +226,14 @@ _SIGS = {
     "gsph_copy_out_async": ([_VP, C.c_int, _VP, C.c_size_t], C.c_int),
     "gsph_checksum": ([_VP, C.POINTER(C.c_double)], C.c_int),
     "gsph_tuning_default": ([C.POINTER(Tuning)], C.c_int),
+    "gsph_server_create": ([C.POINTER(ServerConfig), C.POINTER(_VP)], C.c_int),
+    "gsph_server_destroy": ([_VP], C.c_int),
+    "gsph_server_submit": ([_VP, C.c_uint64, C.POINTER(Params), _VP, _VP, C.c_uint32,
+                            C.c_uint32], C.c_int),
+    "gsph_server_step": ([_VP, C.POINTER(C.c_int)], C.c_int),
+    "gsph_server_poll": ([_VP, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)], C.c_int),
+    "gsph_server_take": ([_VP, C.c_uint64, _VP, _VP], C.c_int),
+    "gsph_server_get_stats": ([_VP, C.POINTER(ServerStats)], C.c_int),
     "gsph_set_render_transform": ([_VP, C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int),
     "gsph_get_tuning": ([_VP, C.POINTER(Tuning)], C.c_int),
     "gsph_set_tuning": ([_VP, C.POINTER(Tuning)], C.c_int),
@@ -536,6 +561,70 @@ class Autotuner:
         t, ms = h.autotune(self.frames, self.candidates)
         self.cache[sig] = (t, ms)
         return t, ms, False
+
+
+class NativeSceneServer:
+    """The native continuous-batching server (gsph_server_*): submit requests
+    from any thread, call step() from one thread, collect finished results
+    with results()."""
+
+    def __init__(self, budget_bytes: int, capacity, chunk: int = 10, device: int = 0):
+        lib = load_library()
+        cfg = ServerConfig(int(budget_bytes), int(capacity[0]), int(capacity[1]),
+                           int(capacity[2]), int(chunk), int(device), 0)
+        h = C.c_void_p()
+        _check(lib.gsph_server_create(C.byref(cfg), C.byref(h)))
+        self._h = h
+        self._lib = lib
+
+    def submit(self, rid: int, params: Params, positions, frames: int, velocities=None):
+        pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 4)
+        vel = None if velocities is None else np.ascontiguousarray(velocities,
+                                                                    np.float32).reshape(-1, 4)
+        _check(self._lib.gsph_server_submit(self._h, rid, C.byref(params),
+                                            _ptr(pos) if len(pos) else None,
+                                            _ptr(vel) if vel is not None and len(vel) else None,
+                                            len(pos), int(frames)))
+
+    def step(self) -> int:
+        k = C.c_int()
+        _check(self._lib.gsph_server_step(self._h, C.byref(k)))
+        return k.value
+
+    def results(self) -> dict:
+        """All finished requests not yet taken: {id: (positions, velocities)}."""
+        out = {}
+        rid, n = C.c_uint64(), C.c_uint32()
+        while self._lib.gsph_server_poll(self._h, C.byref(rid), C.byref(n)) == OK:
+            pos = np.empty((n.value, 4), np.float32)
+            vel = np.empty((n.value, 4), np.float32)
+            _check(self._lib.gsph_server_take(self._h, rid.value,
+                                              _ptr(pos) if n.value else None,
+                                              _ptr(vel) if n.value else None))
+            out[rid.value] = (pos, vel)
+        return out
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(self._lib.gsph_server_get_stats(self._h, C.byref(st)))
+        return st.as_dict()
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.gsph_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def snapshot_info(path: os.PathLike | str) -> dict:

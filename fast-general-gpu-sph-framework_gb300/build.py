@@ -20,7 +20,7 @@ LIB = PKG / "lib"
 ROOT = PKG.parent
 
 CUDA_SOURCES = ["grid.cu", "split.cu", "physics.cu", "system.cu", "noalloc.cu"]
-CXX_SOURCES = ["scene.cpp", "snapshot.cpp"]
+CXX_SOURCES = ["scene.cpp", "snapshot.cpp", "server.cpp"]
 GENCODE = "arch=compute_103a,code=sm_103a"
 
 

@@ -252,6 +252,47 @@ gsph_status gsph_batch_repack(gsph_handle h, const uint32_t *keep, uint32_t n_ke
                               const gsph_params *add_params, const uint32_t *add_counts,
                               uint32_t n_add, const float *add_pos4,
                               const float *add_vel4);
+/* Continuous-batching scene server (no counterpart in the reference, which
+ * steps one scene per process). Requests — a scene's parameters, initial
+ * positions (and velocities) and a number of frames — wait in a FIFO queue;
+ * gsph_server_step admits the queued requests that fit the memory budget and
+ * the batch capacity, steps every resident scene together up to the earliest
+ * completion (at most chunk_frames frames), and keeps the finished requests'
+ * final state for gsph_server_take. Each request is stepped exactly its
+ * frames, and its result is bit-identical to the scene stepped alone. A
+ * request that cannot fit even alone is rejected (counted in the stats).
+ * submit / poll / take / get_stats may be called from other threads while
+ * one thread calls gsph_server_step. All requests share the physical
+ * parameters of the first one admitted (see gsph_batch_create). */
+typedef struct gsph_server *gsph_server_handle;
+typedef struct {
+    uint64_t budget_bytes;         /* device bytes the resident scenes may use */
+    uint64_t particle_capacity;    /* batch capacity: particles, cells, scenes */
+    uint64_t cell_capacity;
+    uint32_t scene_capacity;
+    int32_t chunk_frames;          /* most frames between admissions (>= 1) */
+    int32_t device;
+    int32_t reserved_;
+} gsph_server_config;
+typedef struct {
+    uint64_t submitted, finished, rejected;
+    uint64_t frames, chunks, particle_steps;
+    uint64_t queued, resident, resident_particles, resident_bytes;
+} gsph_server_stats;
+gsph_status gsph_server_create(const gsph_server_config *cfg, gsph_server_handle *out);
+gsph_status gsph_server_destroy(gsph_server_handle s);
+gsph_status gsph_server_submit(gsph_server_handle s, uint64_t id, const gsph_params *p,
+                               const float *pos4, const float *vel4, uint32_t n,
+                               uint32_t frames);
+/* frames_stepped (may be NULL) receives the frames of this chunk (0: idle). */
+gsph_status gsph_server_step(gsph_server_handle s, int *frames_stepped);
+/* The oldest finished request not yet taken (GSPH_ERR_STATE if none). */
+gsph_status gsph_server_poll(gsph_server_handle s, uint64_t *id, uint32_t *n);
+/* Copies a finished request's final positions / velocities (float4 each,
+ * either may be NULL) and releases it. */
+gsph_status gsph_server_take(gsph_server_handle s, uint64_t id, float *pos4, float *vel4);
+gsph_status gsph_server_get_stats(gsph_server_handle s, gsph_server_stats *out);
+
 /* Particle and cell offsets of the scenes: pbase_out[num_scenes + 1],
  * cbase_out[num_scenes + 1] (either may be NULL). Scene k's particles are
  * rows [pbase[k], pbase[k+1]) of every particle field. */
