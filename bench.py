@@ -440,8 +440,13 @@ def run_served(args, ws, rank, local):
     budget = int(args.budget_gb * 1e9)
     # the batch's key space holds 2^26 global cells; particles sized to match
     cap = (args.cap_particles, (1 << 26) - 1, 4096)
-    srv = S.SceneServer(g, budget_bytes=budget, capacity=cap, chunk=args.chunk,
-                        device=local, keep_results=False)
+    native = args.server == "native"
+    if native:
+        srv = g.NativeSceneServer(budget, cap, chunk=args.chunk, device=local)
+        arrivals, finished = {}, {}
+    else:
+        srv = S.SceneServer(g, budget_bytes=budget, capacity=cap, chunk=args.chunk,
+                            device=local, keep_results=False)
     # warm the library (context, modules) on a small scene outside the timed run
     p0, pos0 = W.build(g, {"nx": 16, "ny": 16, "nz": 16, "seed": 3})
     with g.HybridSystem(params=p0, positions=pos0, device=local) as h:
@@ -474,7 +479,11 @@ def run_served(args, ws, rank, local):
                     if dt > 0:
                         time.sleep(dt)
                     p, pos = fut.result()
-                    srv.submit(S.Request(i, p, pos, k, t0 + t_arr))
+                    if native:
+                        arrivals[i] = (t0 + t_arr, len(pos), k)
+                        srv.submit(i, p, pos, k)
+                    else:
+                        srv.submit(S.Request(i, p, pos, k, t0 + t_arr))
         except Exception as e:         # surfaced after the run
             errors.append(e)
         finally:
@@ -487,16 +496,45 @@ def run_served(args, ws, rank, local):
     busy = 0.0
     peak_resident = 0
     peak_particles = 0
-    while not (done_submitting.is_set() and not srv.queue and not srv.resident):
-        tb = time.perf_counter()
-        srv.admit()
-        if srv.resident:
-            peak_resident = max(peak_resident, len(srv.resident))
-            peak_particles = max(peak_particles, sum(r.n for r in srv.resident))
-            srv.step_chunk()
-            busy += time.perf_counter() - tb
-        else:
-            time.sleep(0.001)
+    if native:
+        while True:
+            tb = time.perf_counter()
+            k = srv.step()
+            now = time.perf_counter()
+            for rid in srv.results():
+                finished[rid] = now
+            st = srv.stats()
+            peak_resident = max(peak_resident, st["resident"])
+            peak_particles = max(peak_particles, st["resident_particles"])
+            if k:
+                busy += now - tb
+            elif done_submitting.is_set() and st["queued"] == 0 and st["resident"] == 0:
+                break
+            else:
+                time.sleep(0.001)
+        st = srv.stats()
+        frames, chunks, psteps, rejected = (st["frames"], st["chunks"],
+                                            st["particle_steps"], st["rejected"])
+        from types import SimpleNamespace
+        done = [SimpleNamespace(rid=i, t_arrival=arrivals[i][0], t_done=finished[i])
+                for i in finished]
+        host_s = {"server_steps": busy, "chunks": chunks}
+    else:
+        while not (done_submitting.is_set() and not srv.queue and not srv.resident):
+            tb = time.perf_counter()
+            srv.admit()
+            if srv.resident:
+                peak_resident = max(peak_resident, len(srv.resident))
+                peak_particles = max(peak_particles, sum(r.n for r in srv.resident))
+                srv.step_chunk()
+                busy += time.perf_counter() - tb
+            else:
+                time.sleep(0.001)
+        frames, chunks, psteps, rejected = (srv.frames, srv.chunks, srv.particle_steps,
+                                            len(srv.rejected))
+        done = srv.done
+        host_s = {"step_and_sync": srv.t_step, "repack": srv.t_repack,
+                  "readback": srv.t_readback, "chunks": chunks}
     makespan = time.perf_counter() - t0
     clk = clocks.stop()
     th.join()
@@ -504,14 +542,14 @@ def run_served(args, ws, rank, local):
     if errors:
         raise errors[0]
     makespan = R.max(makespan)
-    served = R.sum(srv.particle_steps) / makespan
-    lat = S.latency_stats(srv.done)
+    served = R.sum(psteps) / makespan
+    lat = S.latency_stats(done)
     offered = sum(sp["nx"] * sp["ny"] * sp["nz"] * k for _, sp, k in trace)
     loop = fifo_loop_model(g, W, trace, local, args.warmup)
     line = {
         "metric": "served aggregate particle-steps/s with p50/p99 completion latency",
-        "value": served, "unit": "particle-steps/s", "n_gpus": ws, "steps": srv.frames,
-        "warmup": args.warmup, "ms_per_step": srv.t_step * 1e3 / max(srv.frames, 1),
+        "value": served, "unit": "particle-steps/s", "n_gpus": ws, "steps": frames,
+        "warmup": args.warmup, "ms_per_step": busy * 1e3 / max(frames, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: seeded Poisson trace of jittered dam-break columns, "
                 "lattices built on arrival",
@@ -519,18 +557,18 @@ def run_served(args, ws, rank, local):
                                f"(Poisson 50/s), N log-uniform [8192, 1048576], "
                                f"K uniform [50, 500]",
                    "budget_gb": args.budget_gb, "capacity_particles": cap[0],
-                   "capacity_cells": cap[1], "chunk_frames": args.chunk},
+                   "capacity_cells": cap[1], "chunk_frames": args.chunk,
+                   "server": "native gsph_server_*" if native else "Python SceneServer"},
         "latency": lat,
-        "requests": len(srv.done), "offered_particle_steps": offered,
+        "requests": len(done), "offered_particle_steps": offered,
         "makespan_s": makespan, "server_busy_s": busy,
-        "host_s": {"step_and_sync": srv.t_step, "repack": srv.t_repack,
-                   "readback": srv.t_readback, "chunks": srv.chunks},
-        "rejected": len(srv.rejected),
+        "host_s": host_s,
+        "rejected": rejected,
         "peak_resident_scenes": peak_resident, "peak_resident_particles": peak_particles,
         "per_scene_fifo_loop": loop,
         "speedup_vs_loop": served / loop["value"],
         "clocks": clk,
-        "gpu_launches": LAUNCHES_PER_FRAME * srv.frames + srv.chunks,
+        "gpu_launches": LAUNCHES_PER_FRAME * frames + chunks,
     }
     if rank == 0:
         print(json.dumps(line))
@@ -558,6 +596,8 @@ def main():
     ap.add_argument("--cap-particles", type=int, default=40_000_000,
                     help="served: particle capacity of the resident batch")
     ap.add_argument("--chunk", type=int, default=10, help="served: frames between admissions")
+    ap.add_argument("--server", default="native", choices=["native", "python"],
+                    help="served: the C++ server (gsph_server_*) or the Python SceneServer")
     ap.add_argument("--stress-side", type=int, default=256, help="stress: column side")
     ap.add_argument("--restart-frames", type=int, default=2000,
                     help="stress: frames before the snapshot")
