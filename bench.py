@@ -6,8 +6,10 @@ force, integrate) over all 3,944,312 particles. Prints ONE JSON line.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
-The GPU arm times K frames with CUDA events on the scene's own stream (state
-resident in HBM, 440 MB > L2, so no L2 flush is needed), samples SM clocks
+The GPU arm times K frames, launched as CUDA graphs of 10 frames, with CUDA
+events on the scene's own stream (state resident in HBM, 440 MB > L2, so no
+L2 flush is needed), takes per-stage times from the frames that follow (stage
+events, frame by frame), samples SM clocks
 during the timed region, measures the end-to-end rate through the public API
 with pinned host buffers, reports the roofline of the dominant kernel and
 times the CPU oracle on the host cores as a reported baseline. The reference
@@ -677,12 +679,14 @@ def measure_scene(g, sysm, args, ws, rank, local, dist, workload, cpu_state):
     n = sysm.n
     stream = torch.cuda.ExternalStream(sysm.stream(), device=torch.device("cuda", local))
 
-    # warm-up (stage timing stays on through the timed region: per-kernel
-    # durations come from events recorded between the stages on this stream)
-    sysm.set_stage_timing(True)
+    # frames run as CUDA graphs of `graph_frames` frames (the library's fastest
+    # launch mode); the warm-up also captures the graph, so no capture falls in
+    # the timed region
+    sysm.set_graph_mode(args.graph_frames)
     sysm.step(max(args.warmup, 0))
+    if args.graph_frames > 0:
+        sysm.step(args.graph_frames)
     sysm.sync()
-    sysm.stage_times()                      # drop warm-up records
 
     clocks = ClockSampler(local)
     ev0 = torch.cuda.Event(enable_timing=True)
@@ -698,6 +702,10 @@ def measure_scene(g, sysm, args, ws, rank, local, dist, workload, cpu_state):
     torch.cuda.synchronize()
     clk = clocks.stop()
     elapsed_ms = ev0.elapsed_time(ev1)
+    # per-stage device times (events between the stages) on the frames right
+    # after the timed ones, launched frame by frame
+    sysm.set_stage_timing(True)
+    sysm.step(max(10, min(args.steps, 50)))
     stages = sysm.stage_times()
     sysm.set_stage_timing(False)
     elapsed_ms = dist.max(elapsed_ms)
@@ -775,7 +783,10 @@ def measure_scene(g, sysm, args, ws, rank, local, dist, workload, cpu_state):
         "config": {"workload": workload, "particles": n,
                    "parallelism": f"{ws} independent replica(s)" if ws > 1 else "single GPU",
                    "l2": f"no flush: {n * 112 / 1e6:.0f} MB particle state per frame > 129 MB L2",
-                   "timing": "CUDA events on the scene stream, stage events inside"},
+                   "timing": "CUDA events on the scene stream around K frames launched "
+                             f"as CUDA graphs of {args.graph_frames} frames; stage times "
+                             "from events between the stages of the frames that follow",
+                   "graph_frames": args.graph_frames},
         "stages_ms": stages,
         "split": {"tra_particles": info.tra_particles, "sms_tasks": info.sms_tasks,
                   "occupied_cells": info.occupied_cells},
