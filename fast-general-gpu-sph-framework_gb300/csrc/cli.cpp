@@ -4,7 +4,7 @@
 // (src/main.cpp:42-85 parseBenchmarkFrames / runHeadlessBenchmark and the print
 // block of HybridSystem::runBenchmark, src/simulation/sph_hybrid_system.cpp:
 // 397-429), plus --scene PATH (the reference compiles the scene path in),
-// --device D and --graph (launch whole frames as CUDA graphs).
+// --device D and --graph (launch whole frames as CUDA graphs of 10 frames).
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -54,7 +54,8 @@ int main(int argc, char **argv) {
     gsph_info info;
     gsph_get_info(h, &info);
     std::printf("Number of particles: %u\n", info.n_particles);
-    if (has_flag(argc, argv, "--graph")) gsph_set_graph_mode(h, 1);
+    // --graph: whole frames launched as CUDA graphs of 10 frames
+    if (has_flag(argc, argv, "--graph")) gsph_set_graph_mode(h, 10);
     gsph_bench_report r;
     st = gsph_benchmark(h, frames, &r);
     if (st) {
