@@ -105,13 +105,17 @@ struct ForceAcc {
     float lap;          // colour laplacian
 };
 
+// kChecked = false for neighbours taken from the density pass's masks: the
+// masks were set by the same squared distance and the same cut-off test, so
+// the test would always pass.
+template <bool kChecked = true>
 __device__ __forceinline__ void force_pair(const float4 &self,
                                            const float4 &sev, const float4 &q,
                                            const float4 &qev,
                                            const DevParams &P, ForceAcc &a) {
     const float rx = self.x - q.x, ry = self.y - q.y, rz = self.z - q.z;
     const float d2 = sq_dist(rx, ry, rz);
-    if (P.h2 < d2 || kFloatSmall > d2) return;
+    if (kChecked && (P.h2 < d2 || kFloatSmall > d2)) return;
     const float inv_d = rsqrtf(d2);
     const float d = d2 * inv_d;
     const float V = q.w;   // 1/rho_j
@@ -574,8 +578,8 @@ k_force_tra(Frame f, DevParams P, bool fresh) {
                 mask &= mask - 1u;
                 const float4 q0 = f.pos[j0], e0 = f.ev[j0];
                 const float4 q1 = f.pos[j1], e1 = f.ev[j1];
-                force_pair(p, pev, q0, e0, P, a);
-                force_pair(p, pev, q1, e1, P, a);
+                force_pair<false>(p, pev, q0, e0, P, a);
+                force_pair<false>(p, pev, q1, e1, P, a);
             }
             if (k < found) {
                 while (!mask) {
@@ -584,7 +588,7 @@ k_force_tra(Frame f, DevParams P, bool fresh) {
                     base = row_start[r][threadIdx.x];
                 }
                 const int j = base + __ffs(mask) - 1;
-                force_pair(p, pev, f.pos[j], f.ev[j], P, a);
+                force_pair<false>(p, pev, f.pos[j], f.ev[j], P, a);
             }
         } else {
             for (int r = 0; r < 9; ++r) {
