@@ -50,6 +50,7 @@ FIELD_TASKS = 11
 FIELD_SPLIT = 12
 FIELD_COLOR = 13
 FIELD_FINAL_POSITION = 14
+FIELD_NEIGHBOR_COUNT = 15
 
 
 class GsphError(RuntimeError):
@@ -441,7 +442,7 @@ class HybridSystem:
             out = np.empty((n, 4), np.float32)
         elif field in (FIELD_KEY, FIELD_COLOR):
             out = np.empty(n, np.uint32)
-        elif field in (FIELD_PERMUTATION, FIELD_COMPACT_INDEX):
+        elif field in (FIELD_PERMUTATION, FIELD_COMPACT_INDEX, FIELD_NEIGHBOR_COUNT):
             out = np.empty(n, np.int32)
         elif field == FIELD_CELL_START:
             out = np.empty(numc + 1, np.int32)

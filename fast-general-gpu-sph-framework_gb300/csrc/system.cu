@@ -861,6 +861,7 @@ size_t field_bytes(const System &s, gsph_field f, gsph_status &st) {
         case GSPH_FIELD_SPLIT: return 8;
         case GSPH_FIELD_COLOR: return N * 4;
         case GSPH_FIELD_FINAL_POSITION: return N * sizeof(float4);
+        case GSPH_FIELD_NEIGHBOR_COUNT: return N * 4;
         case GSPH_FIELD_TASKS: return 0;   // variable, checked separately
     }
     st = GSPH_ERR_INVALID_ARG;
@@ -1278,6 +1279,29 @@ gsph_status gsph_copy_out(gsph_handle h, gsph_field field, void *host_dst,
             GSPH_CUDA(cudaMemcpy(val.data(), s.fr.cell_val, val.size() * sizeof(int4),
                                  cudaMemcpyDeviceToHost));
             for (size_t k = 0; k < occ.size(); ++k) o[occ[k]] = val[k].x;
+            return GSPH_OK;
+        }
+        case GSPH_FIELD_NEIGHBOR_COUNT: {
+            if (!s.arranged) {
+                set_error("gsph_copy_out(NEIGHBOR_COUNT): no arranged frame yet");
+                return GSPH_ERR_STATE;
+            }
+            int32_t *o = static_cast<int32_t *>(host_dst);
+            for (int i = 0; i < s.n; ++i) o[i] = -1;
+            const int mid = std::min(std::max(c.middle, 0), s.n);
+            if (!mid) return GSPH_OK;
+            std::vector<int32_t> flag(static_cast<size_t>(mid)), slot(static_cast<size_t>(mid));
+            GSPH_CUDA(cudaMemcpy(flag.data(), s.fr.nbr_flag, size_t(mid) * 4,
+                                 cudaMemcpyDeviceToHost));
+            if (c.any_sms)
+                GSPH_CUDA(cudaMemcpy(slot.data(), s.fr.compact, size_t(mid) * 4,
+                                     cudaMemcpyDeviceToHost));
+            else
+                for (int i = 0; i < mid; ++i) slot[size_t(i)] = i;
+            for (int i = 0; i < mid; ++i) {
+                const int k = slot[size_t(i)];
+                if (k >= 0 && k < s.n) o[k] = flag[size_t(i)];
+            }
             return GSPH_OK;
         }
         case GSPH_FIELD_SPLIT: {

@@ -179,7 +179,13 @@ typedef enum {
     GSPH_FIELD_COLOR = 13,        /* uint32[N] RGBA8, COLORA of (5000-rho)/6000:
                                      TRA (c,0,c), paired SMS (0,c,c), single
                                      SMS (c,c,0)                              */
-    GSPH_FIELD_FINAL_POSITION = 14 /* float4[N] position * ratio + origin, w=1 */
+    GSPH_FIELD_FINAL_POSITION = 14,/* float4[N] position * ratio + origin, w=1 */
+    /* Diagnostic of the last density pass on the current grid: */
+    GSPH_FIELD_NEIGHBOR_COUNT = 15 /* int32[N] neighbours (0 < d^2 <= h^2) the
+                                     density pass found for each TRA particle;
+                                     -1 for SMS particles and where a
+                                     neighbour row held more than 32
+                                     candidates (no neighbour record)       */
 } gsph_field;
 
 const char *gsph_last_error(void);

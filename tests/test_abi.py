@@ -34,6 +34,15 @@ def test_python_binding_covers_header(gsph):
     assert set(declared_functions()) <= set(gsph._SIGS)
 
 
+def test_field_constants_match_header(gsph):
+    text = (ROOT / "include" / "gsph.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    fields = dict(re.findall(r"\bGSPH_(FIELD_\w+)\s*=\s*(\d+)", text))
+    assert len(fields) >= 16
+    for name, value in fields.items():
+        assert getattr(gsph, name) == int(value), name
+
+
 def test_struct_sizes(gsph):
     assert C.sizeof(gsph.BlockTask) == 32
     assert gsph.load_library().gsph_abi_version() == 1
