@@ -612,8 +612,11 @@ k_force_tra(Frame f, DevParams P, bool fresh) {
 }
 
 // -------------------------------------------------------------- force SMS --
-// One 32-particle task per warp (force_kernels.cu:830-1054). Candidates are
-// staged 64 at a time as structure-of-arrays in shared memory and evaluated
+// One 32-particle task per warp (force_kernels.cu:830-1054). The candidates
+// are the density pass's: x-merged rows, those at dz = -1 / +1 cut to the
+// micro-z groups that can reach the task, one (cell, micro-x slab) segment at
+// a time. They are staged 64 at a time as structure-of-arrays in shared
+// memory and evaluated
 // two at a time with packed FP32x2 arithmetic; a pair is skipped when no lane
 // of the warp interacts with either candidate. Each term rounds as the
 // reference's scalar expression; the two halves of every accumulator are
@@ -648,6 +651,8 @@ k_force_sms(Frame f, DevParams P) {
         const float2 nvx = make_float2(-pev.x, -pev.x);
         const float2 nvy = make_float2(-pev.y, -pev.y);
         const float2 nvz = make_float2(-pev.z, -pev.z);
+        int zmin, zmax;
+        task_z_range(f, self, active, zmin, zmax);
         const float2 pi2 = make_float2(pev.w, pev.w);
         const float2 h2v = make_float2(P.h2, P.h2);
         const float2 hv = make_float2(P.h, P.h);
@@ -663,59 +668,73 @@ k_force_sms(Frame f, DevParams P) {
             const int nz = cz + (r / 3) - 1;
             if (ny < 0 || ny >= G.gy || nz < 0 || nz >= G.gz) continue;
             const int m = G.cbase + cx + G.gx * (ny + G.gy * nz);
-            int begin, end;
-            row_range(f, G, m, cx, task.xxi, task.xxx, begin, end);
-            for (int base = begin; base < end; base += kSmsBatch) {
-                const int cnt = min(kSmsBatch, end - base);
+            // rows at dz = -1 / +1 keep only the micro-z groups that can
+            // reach the task (as the density pass's candidate stream)
+            const int rdz = r / 3 - 1;
+            const int zlo = rdz < 0 ? zmin : 0, zhi = rdz > 0 ? zmax : 3;
+            const bool zcut = f.cell_grp && !(zlo == 0 && zhi == 3);
+            int begin = 0, end = 0;
+            if (!zcut) row_range(f, G, m, cx, task.xxi, task.xxx, begin, end);
+            const int nseg = zcut ? 12 : 1;
+            for (int sg = 0; sg < nseg; ++sg) {
+                if (zcut) {
+                    int sb, sl;
+                    sms_segment(f, G, m, cx, task.xxi, task.xxx, zlo, zhi, sg, sb, sl);
+                    begin = sb;
+                    end = sb + sl;
+                }
+                for (int base = begin; base < end; base += kSmsBatch) {
+                    const int cnt = min(kSmsBatch, end - base);
 #pragma unroll
-                for (int hh = 0; hh < kSmsBatch; hh += 32) {
-                    const int t = hh + lane;
-                    float4 q = make_float4(kFar, kFar, kFar, 0.f);
-                    float4 qv = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (t < cnt) {
-                        q = f.pos[base + t];
-                        qv = f.ev[base + t];
+                    for (int hh = 0; hh < kSmsBatch; hh += 32) {
+                        const int t = hh + lane;
+                        float4 q = make_float4(kFar, kFar, kFar, 0.f);
+                        float4 qv = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (t < cnt) {
+                            q = f.pos[base + t];
+                            qv = f.ev[base + t];
+                        }
+                        sx[t] = q.x; sy[t] = q.y; sz[t] = q.z; sw[t] = q.w;
+                        svx[t] = qv.x; svy[t] = qv.y; svz[t] = qv.z; spr[t] = qv.w;
                     }
-                    sx[t] = q.x; sy[t] = q.y; sz[t] = q.z; sw[t] = q.w;
-                    svx[t] = qv.x; svy[t] = qv.y; svz[t] = qv.z; spr[t] = qv.w;
+                    __syncwarp();
+                    const int pairs = (cnt + 1) >> 1;
+                    for (int k = 0; k < pairs; ++k) {
+                        const float2 dx = __fadd2_rn(reinterpret_cast<const float2 *>(sx)[k], npx);
+                        const float2 dy = __fadd2_rn(reinterpret_cast<const float2 *>(sy)[k], npy);
+                        const float2 dz = __fadd2_rn(reinterpret_cast<const float2 *>(sz)[k], npz);
+                        float2 d2 = __fmul2_rn(dx, dx);
+                        d2 = __ffma2_rn(dy, dy, d2);
+                        d2 = __ffma2_rn(dz, dz, d2);
+                        const float2 t = __ffma2_rn(d2, m1, h2v);   // h^2 - r^2
+                        const bool okx = t.x >= 0.f && d2.x >= kFloatSmall;
+                        const bool oky = t.y >= 0.f && d2.y >= kFloatSmall;
+                        if (!__any_sync(kFull, active && (okx || oky))) continue;
+                        const float2 d2s = make_float2(okx ? d2.x : 1.f, oky ? d2.y : 1.f);
+                        const float2 inv = make_float2(rsqrtf(d2s.x), rsqrtf(d2s.y));
+                        const float2 d = __fmul2_rn(d2s, inv);
+                        const float2 kk = __ffma2_rn(d, m1, hv);       // h - r
+                        const float2 V = reinterpret_cast<const float2 *>(sw)[k];
+                        float2 wk = __fmul2_rn(V, kk);
+                        wk = make_float2(okx ? wk.x : 0.f, oky ? wk.y : 0.f);
+                        const float2 psum = __fadd2_rn(pi2, reinterpret_cast<const float2 *>(spr)[k]);
+                        const float2 ps = __fmul2_rn(__fmul2_rn(__fmul2_rn(wk, psum), kk), inv);
+                        Px = __ffma2_rn(dx, ps, Px);
+                        Py = __ffma2_rn(dy, ps, Py);
+                        Pz = __ffma2_rn(dz, ps, Pz);
+                        Vx = __ffma2_rn(__fadd2_rn(reinterpret_cast<const float2 *>(svx)[k], nvx), wk, Vx);
+                        Vy = __ffma2_rn(__fadd2_rn(reinterpret_cast<const float2 *>(svy)[k], nvy), wk, Vy);
+                        Vz = __ffma2_rn(__fadd2_rn(reinterpret_cast<const float2 *>(svz)[k], nvz), wk, Vz);
+                        float2 wh = __fmul2_rn(V, t);
+                        wh = make_float2(okx ? wh.x : 0.f, oky ? wh.y : 0.f);
+                        const float2 gw = __fmul2_rn(wh, t);
+                        Gx = __ffma2_rn(dx, gw, Gx);
+                        Gy = __ffma2_rn(dy, gw, Gy);
+                        Gz = __ffma2_rn(dz, gw, Gz);
+                        L = __ffma2_rn(wh, __ffma2_rn(t, m075, d2), L);
+                    }
+                    __syncwarp();
                 }
-                __syncwarp();
-                const int pairs = (cnt + 1) >> 1;
-                for (int k = 0; k < pairs; ++k) {
-                    const float2 dx = __fadd2_rn(reinterpret_cast<const float2 *>(sx)[k], npx);
-                    const float2 dy = __fadd2_rn(reinterpret_cast<const float2 *>(sy)[k], npy);
-                    const float2 dz = __fadd2_rn(reinterpret_cast<const float2 *>(sz)[k], npz);
-                    float2 d2 = __fmul2_rn(dx, dx);
-                    d2 = __ffma2_rn(dy, dy, d2);
-                    d2 = __ffma2_rn(dz, dz, d2);
-                    const float2 t = __ffma2_rn(d2, m1, h2v);   // h^2 - r^2
-                    const bool okx = t.x >= 0.f && d2.x >= kFloatSmall;
-                    const bool oky = t.y >= 0.f && d2.y >= kFloatSmall;
-                    if (!__any_sync(kFull, active && (okx || oky))) continue;
-                    const float2 d2s = make_float2(okx ? d2.x : 1.f, oky ? d2.y : 1.f);
-                    const float2 inv = make_float2(rsqrtf(d2s.x), rsqrtf(d2s.y));
-                    const float2 d = __fmul2_rn(d2s, inv);
-                    const float2 kk = __ffma2_rn(d, m1, hv);       // h - r
-                    const float2 V = reinterpret_cast<const float2 *>(sw)[k];
-                    float2 wk = __fmul2_rn(V, kk);
-                    wk = make_float2(okx ? wk.x : 0.f, oky ? wk.y : 0.f);
-                    const float2 psum = __fadd2_rn(pi2, reinterpret_cast<const float2 *>(spr)[k]);
-                    const float2 ps = __fmul2_rn(__fmul2_rn(__fmul2_rn(wk, psum), kk), inv);
-                    Px = __ffma2_rn(dx, ps, Px);
-                    Py = __ffma2_rn(dy, ps, Py);
-                    Pz = __ffma2_rn(dz, ps, Pz);
-                    Vx = __ffma2_rn(__fadd2_rn(reinterpret_cast<const float2 *>(svx)[k], nvx), wk, Vx);
-                    Vy = __ffma2_rn(__fadd2_rn(reinterpret_cast<const float2 *>(svy)[k], nvy), wk, Vy);
-                    Vz = __ffma2_rn(__fadd2_rn(reinterpret_cast<const float2 *>(svz)[k], nvz), wk, Vz);
-                    float2 wh = __fmul2_rn(V, t);
-                    wh = make_float2(okx ? wh.x : 0.f, oky ? wh.y : 0.f);
-                    const float2 gw = __fmul2_rn(wh, t);
-                    Gx = __ffma2_rn(dx, gw, Gx);
-                    Gy = __ffma2_rn(dy, gw, Gy);
-                    Gz = __ffma2_rn(dz, gw, Gz);
-                    L = __ffma2_rn(wh, __ffma2_rn(t, m075, d2), L);
-                }
-                __syncwarp();
             }
         }
         if (active) {
