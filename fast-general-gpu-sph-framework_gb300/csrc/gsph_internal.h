@@ -237,6 +237,9 @@ struct LaunchShape {
 };
 constexpr LaunchShape kMaxShape = {6, 5, 4, 4};   // the kernels' launch bounds
 
+// Shared-memory carveouts of the density and force kernels (once per
+// device, before their first launch).
+cudaError_t configure_physics_kernels(int device);
 void launch_density(const Frame &f, const DevParams &P, int num_sms,
                     const LaunchShape &shape, cudaStream_t s);
 // fresh: the density pass ran on the current state, so the TRA neighbour

@@ -892,7 +892,44 @@ k_final_sum(const double *__restrict__ part, int nparts, double *__restrict__ ou
     block_sum<K>(v, out);
 }
 
+// Shared-memory carveout of one kernel: what `ctas` resident CTAs of it need
+// (static shared memory plus the 1 KB the SM reserves per CTA), so that the
+// rest of the SM's unified L1/shared storage stays L1 for candidate reads.
+template <class Kernel>
+cudaError_t set_carveout(Kernel kernel, int ctas, int smem_per_sm) {
+    cudaFuncAttributes a{};
+    cudaError_t e = cudaFuncGetAttributes(&a, kernel);
+    if (e != cudaSuccess) return e;
+    int pct = 0;
+    if (a.sharedSizeBytes > 0 && smem_per_sm > 0) {
+        const long long need = (long long)(a.sharedSizeBytes + 1024) * ctas;
+        pct = int(std::min<long long>(100, (need * 100 + smem_per_sm - 1) / smem_per_sm));
+    }
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+    if (e != cudaSuccess) return e;
+    // the hint is rounded to a supported split; keep the default if the
+    // rounded one would hold fewer CTAs
+    int fit = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kernel, kWarpsPerBlock * 32, 0);
+    if (e != cudaSuccess) return e;
+    if (fit < ctas)
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 int(cudaSharedmemCarveoutDefault));
+    return e;
+}
+
 }  // namespace
+
+cudaError_t configure_physics_kernels(int device) {
+    int smem = 0;
+    cudaError_t e = cudaDeviceGetAttribute(
+        &smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device);
+    if (e != cudaSuccess) return e;
+    if ((e = set_carveout(k_density_tra, kMaxShape.density_tra, smem))) return e;
+    if ((e = set_carveout(k_density_sms, kMaxShape.density_sms, smem))) return e;
+    if ((e = set_carveout(k_force_tra, kMaxShape.force_tra, smem))) return e;
+    return set_carveout(k_force_sms, kMaxShape.force_sms, smem);
+}
 
 void launch_density(const Frame &f, const DevParams &P, int num_sms,
                     const LaunchShape &shape, cudaStream_t s) {

@@ -266,6 +266,7 @@ struct System {
         device = dev;
         GSPH_CUDA(cudaSetDevice(device));
         num_sms = device_sm_count(device);
+        GSPH_CUDA(configure_physics_kernels(device));
         GSPH_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         long long n_total = 0, c_total = 0;
         if (count < 1) {
