@@ -28,6 +28,10 @@ constexpr int kSmsTaskParticles = 32;
 // Sentinel for cell_xslab: slab boundaries unknown, search the whole cell.
 constexpr uint32_t kXslabUnknown = 0xFFFFFFFFu;
 constexpr uint16_t kGroupsUnknown = 0xFFFFu;
+// Largest particle offset of an SMS task inside its cell: the descriptor's
+// 16-bit p_offset (the reference's field, which wraps past 65,535 particles)
+// plus bits 16-23 in the descriptor's padding byte.
+constexpr int kTaskOffsetLimit = 1 << 24;
 // Neighbour masks of TRA particles: the density pass records, for each of the
 // 9 neighbour rows of a TRA particle, a 32-bit mask of which candidates of the
 // row interact; the force pass walks the set bits instead of re-testing every
@@ -170,6 +174,15 @@ struct Frame {
 };
 
 // ---- shared device helpers (grid sort and the force pass's look-ahead hash) ----
+// Particle offset of an SMS task inside its cell (see kTaskOffsetLimit).
+inline __host__ __device__ int task_offset(const gsph_block_task &t) {
+    return int(t.p_offset) | (int(t.pad_) << 16);
+}
+inline __host__ __device__ void set_task_offset(gsph_block_task &t, int off) {
+    t.p_offset = uint16_t(off & 0xFFFF);
+    t.pad_ = uint8_t(off >> 16);
+}
+
 #ifdef __CUDACC__
 __device__ __forceinline__ unsigned lanemask_lt() {
     unsigned m;

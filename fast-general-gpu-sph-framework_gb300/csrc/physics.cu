@@ -474,9 +474,9 @@ k_density_sms(Frame f, DevParams P) {
         const gsph_block_task task = f.tasks[u];
         const int cb = task.cell_begin;
         const int cend = cb + task.cell_particle_count;
-        const int self = cb + task.p_offset + lane;
+        const int self = cb + task_offset(task) + lane;
         const bool active = self < cend;
-        if (cb + int(task.p_offset) >= cend) continue;   // warp-uniform
+        if (cb + task_offset(task) >= cend) continue;   // warp-uniform
         const float4 p = f.pos[active ? self : cend - 1];
         const SceneGeom G = geom_of_cell(f.scenes, task.cellid);
         int zmin, zmax;
@@ -636,9 +636,9 @@ k_force_sms(Frame f, DevParams P) {
         const gsph_block_task task = f.tasks[u];
         const int cb = task.cell_begin;
         const int cend = cb + task.cell_particle_count;
-        const int self = cb + task.p_offset + lane;
+        const int self = cb + task_offset(task) + lane;
         const bool active = self < cend;
-        if (cb + int(task.p_offset) >= cend) continue;
+        if (cb + task_offset(task) >= cend) continue;
         const int safe = active ? self : cend - 1;
         const float4 p = f.pos[safe];
         const float4 pev = f.ev[safe];
@@ -801,7 +801,7 @@ k_render_sms(Frame f, uint32_t *color) {
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < tasks * kSmsTaskParticles;
          k += gridDim.x * blockDim.x) {
         const gsph_block_task t = f.tasks[k / kSmsTaskParticles];
-        const int i = t.cell_begin + t.p_offset + k % kSmsTaskParticles;
+        const int i = t.cell_begin + task_offset(t) + k % kSmsTaskParticles;
         if (i >= t.cell_begin + t.cell_particle_count) continue;
         const float c = density_color(f, i);
         color[i] = t.is_same ? colora(0.f, c, c, 1.f) : colora(c, c, 0.f, 1.f);

@@ -215,7 +215,7 @@ __host__ __device__ __forceinline__ uint16_t pack_bounds(int min_x, int max_x,
 
 // A7/A8: compact index and task descriptors of each occupied cell.
 __global__ void __launch_bounds__(128)
-k_cell_emit(const int32_t *__restrict__ occ, const Counters *ctr,
+k_cell_emit(const int32_t *__restrict__ occ, Counters *ctr,
             const int32_t *__restrict__ start, const uint32_t *__restrict__ key,
             const int4 *__restrict__ val, const int4 *__restrict__ prefix,
             SceneTable T, int32_t *__restrict__ compact,
@@ -243,6 +243,10 @@ k_cell_emit(const int32_t *__restrict__ occ, const Counters *ctr,
         const int ti = pre.x + t;
         if (ti >= task_count) break;   // capacity guard (error already raised)
         const int off = t * kSmsTaskParticles;
+        if (off >= kTaskOffsetLimit) {   // a cell beyond 2^24 particles
+            atomicOr(&ctr->err, kErrTaskCapacity);
+            break;
+        }
         const uint32_t first_hash = key[b + off];
         const uint32_t last_hash = key[b + min(off + kSmsTaskParticles - 1, n - 1)];
         const int min_x = (first_hash >> 4) & 3, max_x = (last_hash >> 4) & 3;
@@ -250,12 +254,11 @@ k_cell_emit(const int32_t *__restrict__ occ, const Counters *ctr,
         const int min_y = first_hash & 3, max_y = last_hash & 3;
         gsph_block_task task;
         task.is_same = 0;
-        task.pad_ = 0;
         task.cellid = cell;
         task.cell_pos[0] = cx;
         task.cell_pos[1] = cy;
         task.cell_pos[2] = cz;
-        task.p_offset = uint16_t(off);
+        set_task_offset(task, off);
         task.cell_begin = b;
         task.cell_particle_count = n;
         task.xxi = int8_t(min_x);
@@ -295,7 +298,7 @@ __device__ __forceinline__ void judge_pair(gsph_block_task *__restrict__ tasks,
         gsph_block_task t = a;
         a.is_same = 1;
         t.is_same = 1;
-        t.p_offset = uint16_t(a.p_offset + kSmsTaskParticles);
+        set_task_offset(t, task_offset(a) + kSmsTaskParticles);
         tasks[first] = a;
         tasks[second] = t;
         return;

@@ -1716,7 +1716,7 @@ gsph_status gsph_benchmark(gsph_handle h, int frames, gsph_bench_report *out) {
             const gsph_block_task &b = tasks[size_t(i) + 1];
             if (a.is_same) {
                 ++out->is_same_pairs;
-                if (a.cell_particle_count - int(b.p_offset) >= kSmsTaskParticles)
+                if (a.cell_particle_count - task_offset(b) >= kSmsTaskParticles)
                     ++out->full_is_same_pairs;
                 else
                     ++out->partial_is_same_pairs;

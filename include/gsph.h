@@ -101,10 +101,13 @@ typedef struct {
 } gsph_params;
 
 /* BlockTask, the reference's 32-byte SMS task descriptor
- * (particle/particle_buffer.h:60-87), same field layout. */
+ * (particle/particle_buffer.h:60-87), same field layout. p_offset is 16 bits
+ * there and wraps in cells of more than 65,535 particles; here the padding
+ * byte after is_same holds bits 16-23 of the task's particle offset (the
+ * reference leaves that byte undefined), so such cells still run. */
 typedef struct {
     int8_t is_same;
-    uint8_t pad_;
+    uint8_t pad_;                /* bits 16-23 of the particle offset */
     uint16_t paired_bounds;
     int32_t cellid;
     uint16_t cell_pos[3];

@@ -251,6 +251,41 @@ def test_edge_cases(gsph, oracle, cuda_device):
     assert info.big_cells >= 1
 
 
+@pytest.mark.parametrize("count", [6000, 66000])
+def test_crowded_cell_physics_vs_fp64(gsph, oracle, cuda_device, count):
+    """All particles in one coarse cell: past 1,023 particles the cell's
+    micro-x slab boundaries are not recorded (whole-cell TRA rows), past
+    65,535 its (micro-x, micro-z) group offsets are not either (the SMS
+    candidate segments fall back to whole slabs found by the slab words, or
+    the whole cell). Density and force must still match the FP64 oracle.
+    With n neighbours per particle the FP32 sums carry up to (n + 1) u of
+    their magnitude (u = 2^-24), which sets the bounds here."""
+    s, p, _ = dam_scene(gsph, n_side=8)
+    rng = np.random.default_rng(10 + count)
+    h = float(p.kernel)
+    crowd = np.zeros((count, 4), np.float32)
+    crowd[:, :3] = 0.3 + rng.uniform(0.0, h * 0.999, (count, 3))
+    with make(gsph, p, shuffled(crowd)) as sysm:
+        sysm.arrange()
+        cnt = sysm.copy_out(gsph.FIELD_CELL_COUNT)
+        sysm.density()
+        sysm.force()
+        spos = sysm.copy_out(gsph.FIELD_POSITION)
+        sev = sysm.copy_out(gsph.FIELD_EVAL_VELOCITY)
+        acc = sysm.copy_out(gsph.FIELD_ACCELERATION)[:, :3].astype(np.float64)
+        ks = sysm.copy_out(gsph.FIELD_KEY)
+        cs = sysm.copy_out(gsph.FIELD_CELL_START)
+    assert cnt.max() == count
+    u = 2.0 ** -24
+    rho, _ = oracle.density(spos, ks, cs, p)
+    err = np.abs(1.0 / spos[:, 3].astype(np.float64) - rho) / rho
+    assert err.max() <= max(RHO_TOL, (count + 1) * u), err.max()
+    ref, mag = oracle.force(spos, sev, ks, cs, p, with_mag=True)
+    fn = np.linalg.norm(ref, axis=1)
+    dev = np.linalg.norm(acc - ref, axis=1)
+    assert np.all(dev <= FORCE_TOL * fn + (count + 1) * u * mag), (dev / (fn + mag)).max()
+
+
 def test_out_of_domain_reported_not_faulting(gsph, cuda_device):
     s, p, pos = dam_scene(gsph, n_side=8)
     bad = pos.copy()
