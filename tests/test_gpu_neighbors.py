@@ -105,3 +105,51 @@ def test_tra_neighbor_sets_on_pruning_edges(gsph, oracle, cuda_device):
     floor = 1e-3 * np.sqrt(np.mean(fn ** 2))
     dev = np.linalg.norm(acc - ref, axis=1)
     assert np.all(dev <= FORCE_TOL * np.maximum(fn, floor) + FORCE_SUM_TOL * mag)
+
+
+def test_long_rows_fall_back_to_the_candidate_scan(gsph, oracle, cuda_device):
+    """A lone TRA particle whose diagonal neighbour cells are crowded: its
+    (dy, dz) = (-1, -1) row holds more than 32 candidates, so the density
+    pass records no masks for it (neighbour count -1) and the force pass scans
+    its candidates with the cut-off test. Density and force match the FP64
+    oracle."""
+    _, p, _ = dam_scene(gsph, n_side=16)
+    rng = np.random.default_rng(21)
+    cs_ = float(p.cell_size)
+    lone = np.array([[10.25, 10.25, 10.25], [14.6, 14.3, 14.4]]) * cs_
+    crowd = []
+    for base in ([9, 9, 9], [13, 13, 13]):
+        for dx in range(3):
+            c = np.array(base, np.float64) + [dx, 0, 0]
+            crowd.append((c + rng.uniform(0.02, 0.98, (40, 3))) * cs_)
+    xyz = np.concatenate([lone] + crowd).astype(np.float32)
+    pos = np.zeros((len(xyz), 4), np.float32)
+    pos[:, :3] = xyz
+    with gsph.HybridSystem(params=p, positions=shuffled(pos)) as h:
+        h.arrange()
+        h.density()
+        cnt = h.copy_out(gsph.FIELD_NEIGHBOR_COUNT)
+        h.force()
+        spos = h.copy_out(gsph.FIELD_POSITION)
+        sev = h.copy_out(gsph.FIELD_EVAL_VELOCITY)
+        acc = h.copy_out(gsph.FIELD_ACCELERATION)[:, :3].astype(np.float64)
+        ks = h.copy_out(gsph.FIELD_KEY)
+        cs = h.copy_out(gsph.FIELD_CELL_START)
+        split = h.copy_out(gsph.FIELD_SPLIT)
+    is_lone = np.zeros(len(spos), bool)
+    for q in lone.astype(np.float32):
+        is_lone |= np.all(spos[:, :3] == q, axis=1)
+    assert is_lone.sum() == 2
+    assert split[0] >= 2 and split[1] > 0         # TRA and SMS particles both
+    assert np.all(cnt[is_lone] == -1)
+    lo, _ = band_counts(spos, float(np.float32(p.kernel_2)))
+    assert np.all(lo[is_lone] > 0)                # the lone particles interact
+
+    rho, _ = oracle.density(spos, ks, cs, p)
+    gpu_rho = 1.0 / spos[:, 3].astype(np.float64)
+    assert (np.abs(gpu_rho - rho) / rho).max() <= RHO_TOL
+    ref, mag = oracle.force(spos, sev, ks, cs, p, with_mag=True)
+    fn = np.linalg.norm(ref, axis=1)
+    floor = 1e-3 * np.sqrt(np.mean(fn ** 2))
+    dev = np.linalg.norm(acc - ref, axis=1)
+    assert np.all(dev <= FORCE_TOL * np.maximum(fn, floor) + FORCE_SUM_TOL * mag)
