@@ -13,15 +13,17 @@
 //   integrate  src/solver/integration_kernels.cu:235-336 (knIntegrateVelocityE)
 //   checksum   src/simulation/sph_hybrid_system.cpp:43-62
 //
-// Design here: one persistent kernel per pass; each warp repeatedly takes a
-// work unit from a device counter — 32 TRA particles (one per lane) or one
-// 32-particle SMS task (candidates staged 32 at a time in shared memory and
-// broadcast to all lanes). The grid is sized from the SM count, so the launch
-// needs neither the host-side TRA/SMS counts nor a host synchronisation.
-// Neighbour rows merge the three x-adjacent cells of each (dy, dz) row into one
-// contiguous index range, pruned by micro-x slab as in the reference; the
-// interacting neighbours are visited in the same order (rows z-major, then
-// increasing sorted index), so sums match the reference's summation order.
+// Design here: one persistent kernel per pass and path; each warp repeatedly
+// takes a work unit from a device counter — 32 TRA particles (one per lane) or
+// one 32-particle SMS task (candidates staged 64 at a time in shared memory,
+// evaluated two at a time with packed FP32x2 arithmetic by every lane). The
+// grid is sized from the SM count, so the launch needs neither the host-side
+// TRA/SMS counts nor a host synchronisation. Neighbour rows merge the three
+// x-adjacent cells of each (dy, dz) row into one contiguous index range,
+// pruned by micro-x slab as in the reference (SMS rows at dz = -1 / +1 are
+// further cut to the micro-z groups that reach the task). Candidates are
+// visited rows z-major, then in increasing sorted index; the TRA density pass
+// records which interact as bit masks that the TRA force pass walks.
 #include <algorithm>
 
 #include "gsph_internal.h"
