@@ -617,21 +617,22 @@ k_force_tra(Frame f, DevParams P, bool fresh) {
 // One 32-particle task per warp (force_kernels.cu:830-1054). The candidates
 // are the density pass's: x-merged rows, those at dz = -1 / +1 cut to the
 // micro-z groups that can reach the task, one (cell, micro-x slab) segment at
-// a time. They are staged 64 at a time as structure-of-arrays in shared
-// memory and evaluated
-// two at a time with packed FP32x2 arithmetic; a pair is skipped when no lane
-// of the warp interacts with either candidate. Each term rounds as the
-// reference's scalar expression; the two halves of every accumulator are
-// summed at the end.
+// a time. They are staged 64 at a time in shared memory, each candidate pair
+// as four float4s (one 16-byte broadcast load per pair and quantity group),
+// and evaluated two at a time with packed FP32x2 arithmetic; a pair is
+// skipped when no lane of the warp interacts with either candidate. Each
+// term rounds as the reference's scalar expression; the two halves of every
+// accumulator are summed at the end.
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, 4)
 k_force_sms(Frame f, DevParams P) {
-    __shared__ __align__(16) float sm[8][kWarpsPerBlock][kSmsBatch];
+    // candidate pair k (slots 2k, 2k+1) as four float4s: (x, x, y, y),
+    // (z, z, 1/rho, 1/rho), (vx, vx, vy, vy), (vz, vz, p, p)
+    __shared__ __align__(16) float4 sm[4][kWarpsPerBlock][kSmsBatch / 2];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int task_count = f.ctr->task_count;
     if (task_count == 0) return;   // no SMS work: skip the queue atomics
-    float *sx = sm[0][warp], *sy = sm[1][warp], *sz = sm[2][warp], *sw = sm[3][warp];
-    float *svx = sm[4][warp], *svy = sm[5][warp], *svz = sm[6][warp], *spr = sm[7][warp];
+    float4 *sa = sm[0][warp], *sb4 = sm[1][warp], *sc = sm[2][warp], *sd = sm[3][warp];
     for (;;) {
         const int u = next_unit(&f.ctr->work_force_sms);
         if (u >= task_count) break;
@@ -696,15 +697,19 @@ k_force_sms(Frame f, DevParams P) {
                             q = f.pos[base + t];
                             qv = f.ev[base + t];
                         }
-                        sx[t] = q.x; sy[t] = q.y; sz[t] = q.z; sw[t] = q.w;
-                        svx[t] = qv.x; svy[t] = qv.y; svz[t] = qv.z; spr[t] = qv.w;
+                        const int o = (t >> 1) * 4 + (t & 1);
+                        float *fa = reinterpret_cast<float *>(sa), *fb = reinterpret_cast<float *>(sb4);
+                        float *fc = reinterpret_cast<float *>(sc), *fd = reinterpret_cast<float *>(sd);
+                        fa[o] = q.x; fa[o + 2] = q.y; fb[o] = q.z; fb[o + 2] = q.w;
+                        fc[o] = qv.x; fc[o + 2] = qv.y; fd[o] = qv.z; fd[o + 2] = qv.w;
                     }
                     __syncwarp();
                     const int pairs = (cnt + 1) >> 1;
                     for (int k = 0; k < pairs; ++k) {
-                        const float2 dx = __fadd2_rn(reinterpret_cast<const float2 *>(sx)[k], npx);
-                        const float2 dy = __fadd2_rn(reinterpret_cast<const float2 *>(sy)[k], npy);
-                        const float2 dz = __fadd2_rn(reinterpret_cast<const float2 *>(sz)[k], npz);
+                        const float4 qa = sa[k], qb = sb4[k];
+                        const float2 dx = __fadd2_rn(make_float2(qa.x, qa.y), npx);
+                        const float2 dy = __fadd2_rn(make_float2(qa.z, qa.w), npy);
+                        const float2 dz = __fadd2_rn(make_float2(qb.x, qb.y), npz);
                         float2 d2 = __fmul2_rn(dx, dx);
                         d2 = __ffma2_rn(dy, dy, d2);
                         d2 = __ffma2_rn(dz, dz, d2);
@@ -716,17 +721,18 @@ k_force_sms(Frame f, DevParams P) {
                         const float2 inv = make_float2(rsqrtf(d2s.x), rsqrtf(d2s.y));
                         const float2 d = __fmul2_rn(d2s, inv);
                         const float2 kk = __ffma2_rn(d, m1, hv);       // h - r
-                        const float2 V = reinterpret_cast<const float2 *>(sw)[k];
+                        const float2 V = make_float2(qb.z, qb.w);
+                        const float4 qc = sc[k], qd = sd[k];
                         float2 wk = __fmul2_rn(V, kk);
                         wk = make_float2(okx ? wk.x : 0.f, oky ? wk.y : 0.f);
-                        const float2 psum = __fadd2_rn(pi2, reinterpret_cast<const float2 *>(spr)[k]);
+                        const float2 psum = __fadd2_rn(pi2, make_float2(qd.z, qd.w));
                         const float2 ps = __fmul2_rn(__fmul2_rn(__fmul2_rn(wk, psum), kk), inv);
                         Px = __ffma2_rn(dx, ps, Px);
                         Py = __ffma2_rn(dy, ps, Py);
                         Pz = __ffma2_rn(dz, ps, Pz);
-                        Vx = __ffma2_rn(__fadd2_rn(reinterpret_cast<const float2 *>(svx)[k], nvx), wk, Vx);
-                        Vy = __ffma2_rn(__fadd2_rn(reinterpret_cast<const float2 *>(svy)[k], nvy), wk, Vy);
-                        Vz = __ffma2_rn(__fadd2_rn(reinterpret_cast<const float2 *>(svz)[k], nvz), wk, Vz);
+                        Vx = __ffma2_rn(__fadd2_rn(make_float2(qc.x, qc.y), nvx), wk, Vx);
+                        Vy = __ffma2_rn(__fadd2_rn(make_float2(qc.z, qc.w), nvy), wk, Vy);
+                        Vz = __ffma2_rn(__fadd2_rn(make_float2(qd.x, qd.y), nvz), wk, Vz);
                         float2 wh = __fmul2_rn(V, t);
                         wh = make_float2(okx ? wh.x : 0.f, oky ? wh.y : 0.f);
                         const float2 gw = __fmul2_rn(wh, t);
