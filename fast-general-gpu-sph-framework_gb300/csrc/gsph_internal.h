@@ -248,7 +248,7 @@ void launch_split(const Frame &f, const DevParams &P, int max_occ, int num_sms,
 struct LaunchShape {
     int density_tra, density_sms, force_tra, force_sms;
 };
-constexpr LaunchShape kMaxShape = {6, 5, 4, 4};   // the kernels' launch bounds
+constexpr LaunchShape kMaxShape = {6, 4, 4, 4};   // the kernels' launch bounds
 
 // Shared-memory carveouts of the density and force kernels (once per
 // device, before their first launch).

@@ -266,20 +266,6 @@ __device__ __forceinline__ void write_force(const Frame &f, const DevParams &P,
     }
 }
 
-// Squared distances to staged candidates 2k and 2k+1 (x/y/z arrays), as a
-// pair; npx/npy/npz hold the negated self position twice. Same rounding as
-// dx*dx + dy*dy + dz*dz evaluated element by element.
-__device__ __forceinline__ float2 pair_d2(const float *sx, const float *sy,
-                                          const float *sz, int k, float2 npx,
-                                          float2 npy, float2 npz) {
-    const float2 dx = __fadd2_rn(reinterpret_cast<const float2 *>(sx)[k], npx);
-    const float2 dy = __fadd2_rn(reinterpret_cast<const float2 *>(sy)[k], npy);
-    const float2 dz = __fadd2_rn(reinterpret_cast<const float2 *>(sz)[k], npz);
-    float2 d2 = __fmul2_rn(dx, dx);
-    d2 = __ffma2_rn(dy, dy, d2);
-    return __ffma2_rn(dz, dz, d2);
-}
-
 constexpr int kWarpsPerBlock = 8;
 // SMS candidates staged per batch (two per lane).
 constexpr int kSmsBatch = 64;
@@ -457,19 +443,23 @@ __device__ __forceinline__ void task_z_range(const Frame &f, int self, bool acti
 
 // ------------------------------------------------------------ density SMS --
 // One 32-particle task per warp (density_kernels.cu:368-565). Candidates are
-// streamed 64 at a time into x/y/z arrays in shared memory; every lane
-// evaluates them two at a time with packed FP32x2 arithmetic (distances and
-// h^2 - r^2 round exactly as the scalar form).
-__global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
+// streamed 64 at a time into shared memory, each pair (slots 2k, 2k+1) as an
+// (x, x, y, y) float4 and a (z, z) float2; every lane evaluates them two at a
+// time with packed FP32x2 arithmetic (distances and h^2 - r^2 round exactly
+// as the scalar form).
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 4)
 k_density_sms(Frame f, DevParams P) {
-    __shared__ __align__(16) float sms_x[kWarpsPerBlock][kSmsBatch];
-    __shared__ __align__(16) float sms_y[kWarpsPerBlock][kSmsBatch];
-    __shared__ __align__(16) float sms_z[kWarpsPerBlock][kSmsBatch];
+    // candidate pair k (slots 2k, 2k+1): (x, x, y, y) and (z, z)
+    __shared__ __align__(16) float4 sms_xy[kWarpsPerBlock][kSmsBatch / 2];
+    __shared__ __align__(16) float2 sms_zz[kWarpsPerBlock][kSmsBatch / 2];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int task_count = f.ctr->task_count;
     if (task_count == 0) return;   // no SMS work: skip the queue atomics
-    float *sx = sms_x[warp], *sy = sms_y[warp], *sz = sms_z[warp];
+    float *fxy = reinterpret_cast<float *>(sms_xy[warp]);
+    float *fz = reinterpret_cast<float *>(sms_zz[warp]);
+    const float4 *sxy = sms_xy[warp];
+    const float2 *szz = sms_zz[warp];
     for (;;) {
         const int u = next_unit(&f.ctr->work_density_sms);
         if (u >= task_count) break;
@@ -493,19 +483,27 @@ k_density_sms(Frame f, DevParams P) {
             f, G, task, zmin, zmax, lane,
             [&](int slot, int j) {
                 const float4 q = f.pos[j];
-                sx[slot] = q.x;
-                sy[slot] = q.y;
-                sz[slot] = q.z;
+                const int o = (slot >> 1) * 4 + (slot & 1);
+                fxy[o] = q.x;
+                fxy[o + 2] = q.y;
+                fz[slot] = q.z;
             },
             [&](int slot) {
-                sx[slot] = kFar;
-                sy[slot] = kFar;
-                sz[slot] = kFar;
+                const int o = (slot >> 1) * 4 + (slot & 1);
+                fxy[o] = kFar;
+                fxy[o + 2] = kFar;
+                fz[slot] = kFar;
             },
             [&](int pairs) {
 #pragma unroll 4
                 for (int k = 0; k < pairs; ++k) {
-                    const float2 d2 = pair_d2(sx, sy, sz, k, npx, npy, npz);
+                    const float4 qa = sxy[k];
+                    const float2 dx = __fadd2_rn(make_float2(qa.x, qa.y), npx);
+                    const float2 dy = __fadd2_rn(make_float2(qa.z, qa.w), npy);
+                    const float2 dz = __fadd2_rn(szz[k], npz);
+                    float2 d2 = __fmul2_rn(dx, dx);
+                    d2 = __ffma2_rn(dy, dy, d2);
+                    d2 = __ffma2_rn(dz, dz, d2);
                     float2 t = __ffma2_rn(d2, m1, h2v);
                     t.x = (t.x < 0.f || d2.x < kFloatSmall) ? 0.f : t.x;
                     t.y = (t.y < 0.f || d2.y < kFloatSmall) ? 0.f : t.y;
