@@ -307,22 +307,74 @@ __global__ void __launch_bounds__(256) k_sort_small(Frame f) {
     }
 }
 
-// Cells with more than kSmallCellMax particles: one CTA per cell, pairs staged
-// in shared memory (global memory beyond kBigCellSmem), rank by counting.
+// Cells with more than kSmallCellMax particles: one CTA per cell. Pairs
+// compare as (micro cell, source index) inside a cell, so up to kBigCellSmem
+// particles the pairs are staged in shared memory, bucketed by their 6-bit
+// micro cell (counts, scan, scatter) and ranked by value inside their bucket
+// only. Larger cells rank by counting over the whole cell in global memory.
 __global__ void __launch_bounds__(256) k_sort_big(Frame f) {
     __shared__ unsigned long long sp[kBigCellSmem];
+    __shared__ uint16_t order[kBigCellSmem];
+    __shared__ int mcount[64], mfill[64], mstart[65];
     __shared__ int grp[16];
     const int nbig = f.ctr->num_big;
     for (int q = blockIdx.x; q < nbig; q += gridDim.x) {
         const int cell = f.big_list[q];
         const int b = f.cell_start[cell];
         const int cnt = f.cell_start[cell + 1] - b;
-        const bool in_smem = cnt <= kBigCellSmem;
-        if (threadIdx.x < 16) grp[threadIdx.x] = 0;
-        if (in_smem)
+        if (cnt <= kBigCellSmem) {
+            if (threadIdx.x < 64) {
+                mcount[threadIdx.x] = 0;
+                mfill[threadIdx.x] = 0;
+            }
             for (int j = threadIdx.x; j < cnt; j += blockDim.x) sp[j] = f.pairs[b + j];
+            __syncthreads();
+            for (int j = threadIdx.x; j < cnt; j += blockDim.x)
+                atomicAdd(&mcount[int((sp[j] >> 32) & 63ull)], 1);
+            __syncthreads();
+            if (threadIdx.x < 32) {   // exclusive scan of the 64 counts
+                const int l = threadIdx.x;
+                const int c0 = mcount[2 * l], c1 = mcount[2 * l + 1];
+                int x = c0 + c1;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+                    if (l >= o) x += y;
+                }
+                const int excl = x - c0 - c1;
+                mstart[2 * l] = excl;
+                mstart[2 * l + 1] = excl + c0;
+                if (l == 31) mstart[64] = x;
+            }
+            __syncthreads();
+            for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
+                const int m = int((sp[j] >> 32) & 63ull);
+                order[mstart[m] + atomicAdd(&mfill[m], 1)] = uint16_t(j);
+            }
+            __syncthreads();
+            for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+                const unsigned long long e = sp[order[t]];
+                const int m = int((e >> 32) & 63ull);
+                int rank = mstart[m];
+                for (int k = mstart[m]; k < mstart[m + 1]; ++k)
+                    rank += (sp[order[k]] < e) ? 1 : 0;
+                move_particle(f, b + rank, e);
+            }
+            if (threadIdx.x == 0) {
+                int n16[16];
+#pragma unroll
+                for (int g = 0; g < 16; ++g)
+                    n16[g] = mcount[4 * g] + mcount[4 * g + 1] + mcount[4 * g + 2] +
+                             mcount[4 * g + 3];
+                write_groups(f, uint32_t(cell), n16, cnt);
+                f.cell_count[cell] = 0;
+            }
+            __syncthreads();
+            continue;
+        }
+        if (threadIdx.x < 16) grp[threadIdx.x] = 0;
         __syncthreads();
-        const unsigned long long *src = in_smem ? sp : f.pairs + b;
+        const unsigned long long *src = f.pairs + b;
         for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
             const unsigned long long e = src[i];
             int rank = 0;
