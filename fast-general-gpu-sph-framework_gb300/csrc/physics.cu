@@ -251,7 +251,7 @@ __device__ __forceinline__ void write_force(const Frame &f, const DevParams &P,
     ty *= P.mass;
     tz *= P.mass;
     const float4 acc = make_float4(tx + sx, ty + sy, tz + sz, 0.f);
-    f.acc[self] = acc;
+    if (f.acc) f.acc[self] = acc;   // null in the fused frames of a step but its last
     if (f.pos_next) {
         float4 po, vo, eo;
         integrate_one(p, f.vel[self], pev, acc.x, acc.y, acc.z, P, G, po, vo, eo);

@@ -500,9 +500,11 @@ struct System {
     }
     // Force on buffer b with the integration fused in: the new state goes to
     // buffer 1 - b (the previous frame's unsorted copy, no longer read), in
-    // buffer b's order.
-    void enqueue_force_advance(int b) {
+    // buffer b's order. keep_acc: also store the acceleration (the last frame
+    // of a step does, so GSPH_FIELD_ACCELERATION holds it afterwards).
+    void enqueue_force_advance(int b, bool keep_acc = true) {
         Frame f = frame_physics(b);
+        if (!keep_acc) f.acc = nullptr;
         f.pos_next = pos[1 - b];
         f.vel_next = vel[1 - b];
         f.ev_next = ev[1 - b];
@@ -549,7 +551,7 @@ struct System {
         for (int k = 0; k < graph_frames; ++k) {
             enqueue_arrange(parity);
             enqueue_density(1 - parity);
-            enqueue_force_advance(1 - parity);
+            enqueue_force_advance(1 - parity, k == graph_frames - 1);
         }
         cudaError_t e = cudaStreamEndCapture(stream, &g);
         if (e != cudaSuccess) {
@@ -580,7 +582,7 @@ struct System {
     // the force pass, which also integrates, writes the new state back into
     // buffer `cur` in the sorted order. The integrate stage time is then 0
     // (it is part of the force pass).
-    gsph_status tick() {
+    gsph_status tick(bool keep_acc = true) {
         if (numc == 0) return GSPH_OK;   // a batch without scenes
         const int in = cur, out = 1 - cur;
         std::vector<cudaEvent_t> evs;
@@ -592,7 +594,7 @@ struct System {
         if (timing) cudaEventRecord(evs[1], stream);
         enqueue_density(out);
         if (timing) cudaEventRecord(evs[2], stream);
-        enqueue_force_advance(out);
+        enqueue_force_advance(out, keep_acc);
         if (timing) {
             cudaEventRecord(evs[3], stream);
             cudaEventRecord(evs[4], stream);
@@ -633,7 +635,7 @@ struct System {
             }
         }
         for (int k = 0; k < n; ++k) {
-            gsph_status st = tick();
+            gsph_status st = tick(k == n - 1);
             if (st) return st;
         }
         return GSPH_OK;
