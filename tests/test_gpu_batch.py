@@ -78,6 +78,20 @@ def test_batch_rejects_mixed_physics(gsph, cuda_device):
     assert ei.value.status == gsph.ERR_INVALID_ARG
 
 
+def test_batch_rejects_key_space_overflow(gsph, cuda_device):
+    """Cell keys are 32-bit micro keys (cells x 64 < 2^32): a batch whose
+    scenes hold 2^26 cells or more together is refused before any device
+    allocation, although each scene fits alone."""
+    _, p, pos = dam_scene(gsph, n_side=4, box=(6.0, 6.0, 6.0))   # 300^3 cells
+    cells = int(np.prod(list(p.grid_size)))
+    assert cells < 2 ** 26 <= 3 * cells
+    with gsph.Batch([(p, pos)]) as b:          # one scene fits
+        assert b.info().n_cells == cells
+    with pytest.raises(gsph.GsphError) as ei:
+        gsph.Batch([(p, pos)] * 3)
+    assert ei.value.status == gsph.ERR_CAPACITY
+
+
 def test_batch_handles_empty_scene(gsph, cuda_device):
     _, p1, pos1 = dam_scene(gsph, n_side=8)
     _, p2, pos2 = dam_scene(gsph, n_side=9, box=(0.5, 0.4, 0.4))
