@@ -495,7 +495,7 @@ k_density_sms(Frame f, DevParams P) {
                 fz[slot] = kFar;
             },
             [&](int pairs) {
-#pragma unroll 4
+#pragma unroll 32
                 for (int k = 0; k < pairs; ++k) {
                     const float4 qa = sxy[k];
                     const float2 dx = __fadd2_rn(make_float2(qa.x, qa.y), npx);
@@ -703,6 +703,7 @@ k_force_sms(Frame f, DevParams P) {
                     }
                     __syncwarp();
                     const int pairs = (cnt + 1) >> 1;
+#pragma unroll 8
                     for (int k = 0; k < pairs; ++k) {
                         const float4 qa = sa[k], qb = sb4[k];
                         const float2 dx = __fadd2_rn(make_float2(qa.x, qa.y), npx);
@@ -719,10 +720,11 @@ k_force_sms(Frame f, DevParams P) {
                         const float2 inv = make_float2(rsqrtf(d2s.x), rsqrtf(d2s.y));
                         const float2 d = __fmul2_rn(d2s, inv);
                         const float2 kk = __ffma2_rn(d, m1, hv);       // h - r
-                        const float2 V = make_float2(qb.z, qb.w);
+                        // 1/rho of the candidate, zero where it does not interact:
+                        // the pressure, viscosity and colour terms vanish with it
+                        const float2 V = make_float2(okx ? qb.z : 0.f, oky ? qb.w : 0.f);
                         const float4 qc = sc[k], qd = sd[k];
-                        float2 wk = __fmul2_rn(V, kk);
-                        wk = make_float2(okx ? wk.x : 0.f, oky ? wk.y : 0.f);
+                        const float2 wk = __fmul2_rn(V, kk);
                         const float2 psum = __fadd2_rn(pi2, make_float2(qd.z, qd.w));
                         const float2 ps = __fmul2_rn(__fmul2_rn(__fmul2_rn(wk, psum), kk), inv);
                         Px = __ffma2_rn(dx, ps, Px);
@@ -731,8 +733,7 @@ k_force_sms(Frame f, DevParams P) {
                         Vx = __ffma2_rn(__fadd2_rn(make_float2(qc.x, qc.y), nvx), wk, Vx);
                         Vy = __ffma2_rn(__fadd2_rn(make_float2(qc.z, qc.w), nvy), wk, Vy);
                         Vz = __ffma2_rn(__fadd2_rn(make_float2(qd.x, qd.y), nvz), wk, Vz);
-                        float2 wh = __fmul2_rn(V, t);
-                        wh = make_float2(okx ? wh.x : 0.f, oky ? wh.y : 0.f);
+                        const float2 wh = __fmul2_rn(V, t);
                         const float2 gw = __fmul2_rn(wh, t);
                         Gx = __ffma2_rn(dx, gw, Gx);
                         Gy = __ffma2_rn(dy, gw, Gy);
