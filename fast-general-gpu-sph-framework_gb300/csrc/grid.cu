@@ -429,7 +429,7 @@ void launch_scatter_pairs(const Frame &f, cudaStream_t s) {
 void launch_cell_sort(const Frame &f, int num_sms, cudaStream_t s) {
     if (f.n <= 0) return;
     k_sort_small<<<(f.n + 255) / 256, 256, 0, s>>>(f);
-    k_sort_big<<<num_sms * 2, 256, 0, s>>>(f);
+    k_sort_big<<<num_sms * 4, 256, 0, s>>>(f);
 }
 
 }  // namespace gsph
