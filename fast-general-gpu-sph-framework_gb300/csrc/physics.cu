@@ -15,7 +15,7 @@
 //
 // Design here: one persistent kernel per pass and path; each warp repeatedly
 // takes a work unit from a device counter — 32 TRA particles (one per lane) or
-// one 32-particle SMS task (candidates staged 64 at a time in shared memory,
+// one 32-particle SMS task (candidates staged in batches in shared memory,
 // evaluated two at a time with packed FP32x2 arithmetic by every lane). The
 // grid is sized from the SM count, so the launch needs neither the host-side
 // TRA/SMS counts nor a host synchronisation. Neighbour rows merge the three
@@ -269,6 +269,7 @@ __device__ __forceinline__ void write_force(const Frame &f, const DevParams &P,
 constexpr int kWarpsPerBlock = 8;
 // SMS candidates staged per batch (two per lane).
 constexpr int kSmsBatch = 64;
+constexpr int kDenBatch = 256;   // SMS density: candidates staged per batch
 // Coordinate of padding candidates: far outside any kernel radius.
 constexpr float kFar = 1.0e18f;
 
@@ -378,7 +379,7 @@ __device__ __forceinline__ void sms_segment(const Frame &f, const SceneGeom &G, 
     }
 }
 
-// Streams a task's candidates through a warp's 64-slot staging batch:
+// Streams a task's candidates through a warp's kDenBatch-slot staging batch:
 // stage(slot, index) fills one slot, run(pairs) evaluates the staged slots
 // two at a time; batches run full except the last (its odd slot is padded
 // by pad(slot)). Control flow is warp-uniform.
@@ -392,13 +393,13 @@ __device__ __forceinline__ void sms_stream(const Frame &f, const SceneGeom &G,
     auto take_range = [&](int b, int len) {
         int o = 0;
         while (o < len) {
-            const int n = min(len - o, kSmsBatch - fill);
+            const int n = min(len - o, kDenBatch - fill);
             for (int t = lane; t < n; t += 32) stage(fill + t, b + o + t);
             fill += n;
             o += n;
-            if (fill == kSmsBatch) {
+            if (fill == kDenBatch) {
                 __syncwarp();
-                run(kSmsBatch / 2);
+                run(kDenBatch / 2);
                 __syncwarp();
                 fill = 0;
             }
@@ -443,15 +444,15 @@ __device__ __forceinline__ void task_z_range(const Frame &f, int self, bool acti
 
 // ------------------------------------------------------------ density SMS --
 // One 32-particle task per warp (density_kernels.cu:368-565). Candidates are
-// streamed 64 at a time into shared memory, each pair (slots 2k, 2k+1) as an
+// streamed 256 at a time into shared memory, each pair (slots 2k, 2k+1) as an
 // (x, x, y, y) float4 and a (z, z) float2; every lane evaluates them two at a
 // time with packed FP32x2 arithmetic (distances and h^2 - r^2 round exactly
 // as the scalar form).
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, 4)
 k_density_sms(Frame f, DevParams P) {
     // candidate pair k (slots 2k, 2k+1): (x, x, y, y) and (z, z)
-    __shared__ __align__(16) float4 sms_xy[kWarpsPerBlock][kSmsBatch / 2];
-    __shared__ __align__(16) float2 sms_zz[kWarpsPerBlock][kSmsBatch / 2];
+    __shared__ __align__(16) float4 sms_xy[kWarpsPerBlock][kDenBatch / 2];
+    __shared__ __align__(16) float2 sms_zz[kWarpsPerBlock][kDenBatch / 2];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int task_count = f.ctr->task_count;
