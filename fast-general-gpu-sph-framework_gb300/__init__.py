@@ -216,6 +216,7 @@ _SIGS = {
     "gsph_density": ([_VP], C.c_int),
     "gsph_force": ([_VP], C.c_int),
     "gsph_advance": ([_VP], C.c_int),
+    "gsph_step_host_async": ([_VP, C.c_int, _VP, _VP, _VP], C.c_int),
     "gsph_set_graph_mode": ([_VP, C.c_int], C.c_int),
     "gsph_sync": ([_VP], C.c_int),
     "gsph_stream": ([_VP, C.POINTER(_VP)], C.c_int),
@@ -404,6 +405,11 @@ class HybridSystem:
 
     def copy_in_async(self, field: int, host_ptr: int, nbytes: int) -> None:
         _check(self._lib.gsph_copy_in_async(self._h, field, host_ptr, nbytes))
+
+    def step_host_async(self, frames: int, pos_ptr: int, vel_ptr: int, ev_ptr: int) -> None:
+        """gsph_step_host_async: pinned host state in, `frames` frames, state out
+        into the same arrays (complete after sync())."""
+        _check(self._lib.gsph_step_host_async(self._h, int(frames), pos_ptr, vel_ptr, ev_ptr))
 
     def copy_out_async(self, field: int, host_ptr: int, nbytes: int) -> None:
         _check(self._lib.gsph_copy_out_async(self._h, field, host_ptr, nbytes))

@@ -120,6 +120,21 @@ struct System {
 
     bool timing = false;
     std::vector<cudaEvent_t> ev_pool;
+
+    // gsph_step_host_async: the state's return copies run on their own
+    // stream, one event per array, so that the next call's upload of an array
+    // waits only for that array's return copy. Every other entry point joins
+    // them into the main stream first (join_xfer).
+    cudaStream_t xfer = nullptr;
+    cudaEvent_t xfer_done[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t frames_done = nullptr;
+    bool xfer_pending = false;
+
+    void join_xfer() {
+        if (!xfer_pending) return;
+        for (cudaEvent_t e : xfer_done) cudaStreamWaitEvent(stream, e, 0);
+        xfer_pending = false;
+    }
     std::vector<std::vector<cudaEvent_t>> ev_pending;   // 5 events per frame
 
     ~System() { release(); }
@@ -136,6 +151,21 @@ struct System {
         ev_pending.clear();
         for (auto e : ev_pool) cudaEventDestroy(e);
         ev_pool.clear();
+        if (xfer) {
+            cudaStreamSynchronize(xfer);
+            cudaStreamDestroy(xfer);
+            xfer = nullptr;
+        }
+        for (auto &e : xfer_done)
+            if (e) {
+                cudaEventDestroy(e);
+                e = nullptr;
+            }
+        if (frames_done) {
+            cudaEventDestroy(frames_done);
+            frames_done = nullptr;
+        }
+        xfer_pending = false;
         for (void *p : allocs) cudaFree(p);
         allocs.clear();
         if (stream) {
@@ -649,6 +679,7 @@ struct System {
     }
 
     gsph_status sync_and_check() {
+        join_xfer();
         GSPH_CUDA(cudaStreamSynchronize(stream));
         Counters c;
         gsph_status st = read_counters(c);
@@ -832,7 +863,10 @@ struct gsph_system {
 
 namespace {
 
-gsph_status check_handle(gsph_handle h) {
+// Validates the handle and makes it current. join: order the main stream
+// after any state return copies still in flight (every entry point but
+// gsph_step_host_async, which waits array by array).
+gsph_status check_handle(gsph_handle h, bool join = true) {
     if (!h) {
         set_error("null gsph handle");
         return GSPH_ERR_INVALID_ARG;
@@ -843,6 +877,7 @@ gsph_status check_handle(gsph_handle h) {
                   cudaGetErrorString(e));
         return GSPH_ERR_CUDA;
     }
+    if (join) h->sys.join_xfer();
     return GSPH_OK;
 }
 
@@ -1449,6 +1484,51 @@ gsph_status gsph_copy_in_async(gsph_handle h, gsph_field field,
         s.grid_current = false;
         s.hashed = false;
     }
+    return GSPH_OK;
+}
+
+gsph_status gsph_step_host_async(gsph_handle h, int frames, void *pos4, void *vel4,
+                                 void *ev4) {
+    gsph_status st = check_handle(h, false);
+    if (st) return st;
+    System &s = h->sys;
+    if (frames < 0 || !pos4 || !vel4 || !ev4) {
+        set_error("gsph_step_host_async: negative frame count or null array");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    if (!s.xfer) {
+        GSPH_CUDA(cudaStreamCreateWithFlags(&s.xfer, cudaStreamNonBlocking));
+        for (auto &e : s.xfer_done)
+            GSPH_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        GSPH_CUDA(cudaEventCreateWithFlags(&s.frames_done, cudaEventDisableTiming));
+    }
+    const gsph_field fields[3] = {GSPH_FIELD_POSITION, GSPH_FIELD_VELOCITY,
+                                  GSPH_FIELD_EVAL_VELOCITY};
+    void *host[3] = {pos4, vel4, ev4};
+    const size_t bytes = size_t(s.n) * sizeof(float4);
+    // upload: each array after its previous return copy (if any) is done
+    for (int k = 0; k < 3; ++k) {
+        if (s.xfer_pending) GSPH_CUDA(cudaStreamWaitEvent(s.stream, s.xfer_done[k], 0));
+        if (bytes)
+            GSPH_CUDA(cudaMemcpyAsync(state_ptr(s, fields[k]), host[k], bytes,
+                                      cudaMemcpyHostToDevice, s.stream));
+    }
+    s.xfer_pending = false;
+    s.lists_valid = false;
+    s.grid_current = false;
+    s.hashed = false;
+    if ((st = s.step(frames))) return st;
+    if ((st = s.check_launch())) return st;
+    // return copies on the transfer stream, after the frames
+    GSPH_CUDA(cudaEventRecord(s.frames_done, s.stream));
+    GSPH_CUDA(cudaStreamWaitEvent(s.xfer, s.frames_done, 0));
+    for (int k = 0; k < 3; ++k) {
+        if (bytes)
+            GSPH_CUDA(cudaMemcpyAsync(host[k], state_ptr(s, fields[k]), bytes,
+                                      cudaMemcpyDeviceToHost, s.xfer));
+        GSPH_CUDA(cudaEventRecord(s.xfer_done[k], s.xfer));
+    }
+    s.xfer_pending = true;
     return GSPH_OK;
 }
 

@@ -347,6 +347,16 @@ gsph_status gsph_copy_in_async(gsph_handle h, gsph_field field,
                                const void *host_src, size_t bytes);
 gsph_status gsph_copy_out_async(gsph_handle h, gsph_field field,
                                 void *host_dst, size_t bytes);
+/* A step on host-resident state: uploads position, velocity and evaluated
+ * velocity (float4[N] each, the handle's current order, pinned memory) from
+ * the three arrays, runs `frames` frames and downloads the new state into the
+ * same arrays (HybridSystem::tick with the state kept on the host). Asynchronous:
+ * the arrays are complete after gsph_sync. The downloads run on an internal
+ * stream, so the upload of an array by the next call waits only for that
+ * array's own download (the three round trips overlap); every other call on
+ * the handle first waits for all of them. */
+gsph_status gsph_step_host_async(gsph_handle h, int frames, void *pos4, void *vel4,
+                                 void *ev4);
 
 /* Render-space transform of GSPH_FIELD_FINAL_POSITION (the reference's
  * sim_ratio / sim_origin, sph_hybrid_system.cpp:221-224); default ratio 1,
