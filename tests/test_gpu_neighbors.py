@@ -153,3 +153,38 @@ def test_long_rows_fall_back_to_the_candidate_scan(gsph, oracle, cuda_device):
     floor = 1e-3 * np.sqrt(np.mean(fn ** 2))
     dev = np.linalg.norm(acc - ref, axis=1)
     assert np.all(dev <= FORCE_TOL * np.maximum(fn, floor) + FORCE_SUM_TOL * mag)
+
+
+@pytest.mark.parametrize("per_cell", [8, 12, 16, 150])
+def test_random_mixed_split_vs_fp64(gsph, oracle, cuda_device, per_cell):
+    """Uniform random positions at 8 / 12 / 16 / 150 particles per cell: the
+    performance model sends from a few to all cells to SMS tasks and the rest
+    to TRA, with TRA rows both shorter and longer than 32 candidates. Density
+    and force match the FP64 oracle within the parity bounds."""
+    _, p, _ = dam_scene(gsph, n_side=16)
+    rng = np.random.default_rng(per_cell)
+    lo, hi = 0.06, 0.26                           # 10 cells a side
+    n = int(per_cell * ((hi - lo) / p.cell_size) ** 3)
+    pos = np.zeros((n, 4), np.float32)
+    pos[:, :3] = rng.uniform(lo, hi, (n, 3))
+    with gsph.HybridSystem(params=p, positions=pos) as h:
+        h.arrange()
+        split = h.copy_out(gsph.FIELD_SPLIT)
+        h.density()
+        h.force()
+        spos = h.copy_out(gsph.FIELD_POSITION)
+        sev = h.copy_out(gsph.FIELD_EVAL_VELOCITY)
+        acc = h.copy_out(gsph.FIELD_ACCELERATION)[:, :3].astype(np.float64)
+        ks = h.copy_out(gsph.FIELD_KEY)
+        cs = h.copy_out(gsph.FIELD_CELL_START)
+    assert split[1] > 0, "some cells must go to SMS tasks"
+    if per_cell <= 16:
+        assert split[0] > 0, "some particles must stay on TRA"
+    rho, _ = oracle.density(spos, ks, cs, p)
+    gpu_rho = 1.0 / spos[:, 3].astype(np.float64)
+    assert (np.abs(gpu_rho - rho) / rho).max() <= RHO_TOL
+    ref, mag = oracle.force(spos, sev, ks, cs, p, with_mag=True)
+    fn = np.linalg.norm(ref, axis=1)
+    floor = 1e-3 * np.sqrt(np.mean(fn ** 2))
+    dev = np.linalg.norm(acc - ref, axis=1)
+    assert np.all(dev <= FORCE_TOL * np.maximum(fn, floor) + FORCE_SUM_TOL * mag)
