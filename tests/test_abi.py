@@ -43,6 +43,32 @@ def test_field_constants_match_header(gsph):
         assert getattr(gsph, name) == int(value), name
 
 
+def test_header_is_c99_and_links(gsph, tmp_path):
+    """include/gsph.h compiles as strict C99 with warnings as errors, and a C
+    program links against libgsph.so and calls into it (no GPU needed)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "abi.c"
+    src.write_text(
+        '#include "gsph.h"\n#include <stdio.h>\n'
+        "int main(void) {\n"
+        "    gsph_tuning t;\n"
+        "    if (gsph_tuning_default(&t) != GSPH_OK) return 2;\n"
+        '    printf("%d %d %d\\n", (int)sizeof(gsph_block_task), gsph_abi_version(),\n'
+        "           t.sparse_total);\n"
+        "    return 0;\n}\n")
+    lib = gsph.LIB_PATH.parent
+    exe = tmp_path / "abi"
+    subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror",
+                    f"-I{ROOT / 'include'}", str(src), f"-L{lib}", "-lgsph",
+                    f"-Wl,-rpath,{lib}", "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    assert out.split() == ["32", "1", "96"]
+
+
 def test_struct_sizes(gsph):
     assert C.sizeof(gsph.BlockTask) == 32
     assert gsph.load_library().gsph_abi_version() == 1
