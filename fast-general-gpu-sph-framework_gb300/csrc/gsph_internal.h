@@ -271,6 +271,13 @@ void launch_checksum(const float4 *pos, int n, double *out5, cudaStream_t s);
 
 // Host-side helpers (scene.cpp).
 DevParams make_dev_params(const gsph_params &p);
+// Checks a scene's grid before any kernel sees it: every dimension in
+// [1, 65535] and the cell count, computed in 64 bits, below kMaxCells (32-bit
+// micro keys hold the cell index in their upper 26 bits). On success stores
+// the cell count in *numc; otherwise sets the error string (prefixed by
+// `who`) and returns GSPH_ERR_INVALID_ARG or GSPH_ERR_CAPACITY.
+constexpr long long kMaxCells = 1LL << 26;
+gsph_status check_grid(const gsph_params &p, const char *who, long long *numc);
 SceneGeom make_scene_geom(const gsph_params &p, int cbase);
 void set_error(const char *fmt, ...);
 

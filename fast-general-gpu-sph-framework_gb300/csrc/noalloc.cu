@@ -17,6 +17,8 @@
 // This entry point has no counterpart in the reference.
 #include <mutex>
 
+#include <cuda.h>
+
 #include "gsph_internal.h"
 
 namespace gsph {
@@ -30,26 +32,73 @@ static __device__ __align__(256) unsigned char
     g_sort_scratch[GSPH_NOALLOC_SCRATCH_BYTES];
 
 std::mutex g_scratch_mutex;
-void *g_scratch_addr[kMaxDevices] = {};
+// Per device: the address of g_sort_scratch and the unique ID of the CUDA
+// context it was looked up in. A context ID is never reused within a process,
+// so a cudaDeviceReset (which unloads the module with its context) or a
+// different current context (a non-primary driver context) forces a new
+// look-up instead of reusing an address of another context.
+struct ScratchCache {
+    unsigned long long ctx_id;
+    void *addr;
+};
+ScratchCache g_scratch[kMaxDevices] = {};
 
-// Device address of g_sort_scratch on the current device. The array's name
-// in host code is only a host-side stand-in, so the address is looked up once
-// per device, with that device current, and cached.
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
+
+// Unique ID of the current context, or 0 where none is current or the driver
+// does not report one (then every call looks the address up again).
+unsigned long long current_context_id() {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static bool resolved = false;
+    if (!resolved) {
+        resolved = true;
+        void *fa = nullptr, *fb = nullptr;
+        cudaDriverEntryPointQueryResult qa, qb;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fa, 12000,
+                                             cudaEnableDefault, &qa) == cudaSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &fb, 12000,
+                                             cudaEnableDefault, &qb) == cudaSuccess &&
+            qa == cudaDriverEntryPointSuccess && qb == cudaDriverEntryPointSuccess) {
+            get_current = reinterpret_cast<CtxGetCurrentFn>(fa);
+            get_id = reinterpret_cast<CtxGetIdFn>(fb);
+        }
+        cudaGetLastError();
+    }
+    if (!get_current || !get_id) return 0;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+    if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of g_sort_scratch in the current context. In host code the
+// array's name is only a host-side stand-in, so the address is looked up with
+// the device current — once per device and context: the first call on a
+// device (and the first after a device reset) does this set-up.
 gsph_status scratch_address(int device, void **out) {
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_addr[device]) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_sort_scratch);
-        if (e != cudaSuccess || !p) {
-            cudaGetLastError();
-            set_error("gsph_grid_sort_dev_noalloc: cudaGetSymbolAddress failed "
-                      "on device %d: %s",
-                      device, cudaGetErrorString(e));
-            return GSPH_ERR_CUDA;
-        }
-        g_scratch_addr[device] = p;
+    ScratchCache &c = g_scratch[device];
+    const unsigned long long id = current_context_id();
+    if (id != 0 && c.addr && c.ctx_id == id) {
+        *out = c.addr;
+        return GSPH_OK;
     }
-    *out = g_scratch_addr[device];
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_sort_scratch);
+    if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        set_error("gsph_grid_sort_dev_noalloc: cudaGetSymbolAddress failed "
+                  "on device %d: %s",
+                  device, cudaGetErrorString(e));
+        return GSPH_ERR_CUDA;
+    }
+    // the look-up made the context current if it was not yet
+    c.ctx_id = id != 0 ? id : current_context_id();
+    c.addr = p;
+    *out = p;
     return GSPH_OK;
 }
 
@@ -67,10 +116,12 @@ extern "C" gsph_status gsph_grid_sort_dev_noalloc(
         set_error("gsph_grid_sort_dev_noalloc: null parameters");
         return GSPH_ERR_INVALID_ARG;
     }
-    const long long numc = (long long)p->grid_size[0] * p->grid_size[1] *
-                           p->grid_size[2];
-    if (n > GSPH_NOALLOC_MAX_PARTICLES || numc > GSPH_NOALLOC_MAX_CELLS ||
-        numc <= 0) {
+    long long numc = 0;
+    {
+        const gsph_status gs = check_grid(*p, "gsph_grid_sort_dev_noalloc", &numc);
+        if (gs) return gs;
+    }
+    if (n > GSPH_NOALLOC_MAX_PARTICLES || numc > GSPH_NOALLOC_MAX_CELLS) {
         set_error("gsph_grid_sort_dev_noalloc: %u particles and %lld cells "
                   "exceed the fixed scratch (at most %u particles and %u "
                   "cells); use gsph_grid_sort_dev with caller scratch",

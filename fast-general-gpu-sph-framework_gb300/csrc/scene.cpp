@@ -240,6 +240,24 @@ DevParams make_dev_params(const gsph_params &p) {
     return d;
 }
 
+gsph_status check_grid(const gsph_params &p, const char *who, long long *numc) {
+    for (int a = 0; a < 3; ++a) {
+        if (p.grid_size[a] < 1 || p.grid_size[a] > 65535) {
+            set_error("%s: grid size %d along axis %d out of range [1, 65535]",
+                      who, int(p.grid_size[a]), a);
+            return GSPH_ERR_INVALID_ARG;
+        }
+    }
+    const long long c =
+        (long long)p.grid_size[0] * p.grid_size[1] * p.grid_size[2];
+    if (c >= kMaxCells) {
+        set_error("%s: grid has %lld cells; at most 2^26 - 1 are supported", who, c);
+        return GSPH_ERR_CAPACITY;
+    }
+    if (numc) *numc = c;
+    return GSPH_OK;
+}
+
 SceneGeom make_scene_geom(const gsph_params &p, int cbase) {
     SceneGeom g{};
     g.gx = p.grid_size[0];

@@ -945,11 +945,9 @@ gsph_status gsph_create(const gsph_params *p, const float *pos4,
         set_error("device %d out of range [0, %d)", device, count);
         return GSPH_ERR_INVALID_ARG;
     }
-    const int numc = p->grid_size[0] * p->grid_size[1] * p->grid_size[2];
-    if (numc <= 0 || p->grid_size[0] <= 0 || p->grid_size[1] <= 0 ||
-        p->grid_size[2] <= 0) {
-        set_error("gsph_create: empty grid");
-        return GSPH_ERR_INVALID_ARG;
+    {
+        const gsph_status gs = check_grid(*p, "gsph_create", nullptr);
+        if (gs) return gs;
     }
     gsph_system *h = new (std::nothrow) gsph_system();
     if (!h) {
@@ -1843,9 +1841,13 @@ gsph_status gsph_grid_sort_dev(const gsph_params *p, uint32_t n,
         set_error("gsph_grid_sort_dev: null argument");
         return GSPH_ERR_INVALID_ARG;
     }
+    {
+        const gsph_status gs = check_grid(*p, "gsph_grid_sort_dev", nullptr);
+        if (gs) return gs;
+    }
     const DevParams dp = make_dev_params(*p);
-    if (dp.numc <= 0 || n > 0x7FFFFFFFu) {
-        set_error("gsph_grid_sort_dev: empty grid or too many particles");
+    if (n > 0x7FFFFFFFu) {
+        set_error("gsph_grid_sort_dev: too many particles");
         return GSPH_ERR_INVALID_ARG;
     }
     const size_t need = gsph_grid_sort_scratch_bytes(n, uint32_t(dp.numc));

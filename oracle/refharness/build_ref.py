@@ -11,6 +11,7 @@ is compiled next to it. Outputs go to oracle/_ref/ only (git-ignored).
 """
 from __future__ import annotations
 
+import os
 import shutil
 import subprocess
 from pathlib import Path
@@ -18,7 +19,9 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
 OUT = ROOT / "oracle" / "_ref"
-REFERENCE_SRC = Path("/root/reference/src")
+# The reference tree's src/ directory: GSPH_REFERENCE_SRC, else the
+# development container's checkout.
+REFERENCE_SRC = Path(os.environ.get("GSPH_REFERENCE_SRC", "/root/reference/src"))
 CUBIN = OUT / "ref_device.cubin"
 HARNESS = OUT / "ref_harness"
 GENCODE = "arch=compute_103a,code=sm_103a"

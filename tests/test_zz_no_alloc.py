@@ -83,6 +83,47 @@ def test_noalloc_grid_sort_matches_allocating_sort(gsph, cuda_device):
         assert np.array_equal(b["pos"], pos[b["perm"]])
 
 
+def test_noalloc_at_the_declared_maximum(gsph, cuda_device):
+    """The 262,144-particle dam break over its 128 x 64 x 64 = 524,288-cell grid
+    is exactly the declared maximum: the scratch layout then fills the array."""
+    import torch
+
+    lib = gsph.load_library()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    s = gsph.load_scene(gsph.scene_path("dam_break_262k.json"))
+    p = gsph.params_init(s)
+    base = gsph.lattice(s, p)
+    n, numc = len(base), p.numc
+    assert n == gsph_max(lib, "particles") and numc == gsph_max(lib, "cells")
+    stream = torch.cuda.current_stream().cuda_stream
+    pos = shuffled(base, seed=7)
+    vel = np.zeros_like(pos)
+    pin, vin = (torch.from_numpy(a).to(dev) for a in (pos, vel))
+    ref = _outputs(torch, n, numc, dev)
+    nbytes = lib.gsph_grid_sort_scratch_bytes(n, numc)
+    scratch = torch.empty(nbytes + 256, dtype=torch.uint8, device=dev)
+    base_ptr = (scratch.data_ptr() + 255) // 256 * 256
+    st = lib.gsph_grid_sort_dev(C.byref(p), n, pin.data_ptr(), vin.data_ptr(),
+                                vin.data_ptr(), ref["pos"].data_ptr(), ref["vel"].data_ptr(),
+                                ref["ev"].data_ptr(), ref["key"].data_ptr(),
+                                ref["perm"].data_ptr(), ref["cs"].data_ptr(), base_ptr,
+                                nbytes, stream)
+    assert st == 0, lib.gsph_last_error()
+    for call in range(2):
+        out = _outputs(torch, n, numc, dev)
+        st = lib.gsph_grid_sort_dev_noalloc(C.byref(p), n, pin.data_ptr(), vin.data_ptr(),
+                                            vin.data_ptr(), out["pos"].data_ptr(),
+                                            out["vel"].data_ptr(), out["ev"].data_ptr(),
+                                            out["key"].data_ptr(), out["perm"].data_ptr(),
+                                            out["cs"].data_ptr(), stream)
+        assert st == 0, lib.gsph_last_error()
+        torch.cuda.synchronize()
+        a, b = _host(ref), _host(out)
+        for k in a:
+            assert np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32)), (call, k)
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch(gsph, cuda_device):
     import torch
 
