@@ -409,6 +409,44 @@ static void dump(const std::string &dir, const char *name, const void *dptr,
     std::fprintf(meta, "%s %s %zu %d\n", name, dtype, count / size_t(cols), cols);
 }
 
+static void write_host(const std::string &dir, const char *name, const void *h,
+                       size_t bytes, size_t rows, FILE *meta, const char *dtype) {
+    const std::string path = dir + "/" + name + ".bin";
+    FILE *f = std::fopen(path.c_str(), "wb");
+    if (!f) {
+        std::fprintf(stderr, "cannot write %s\n", path.c_str());
+        std::exit(2);
+    }
+    if (bytes) std::fwrite(h, 1, bytes, f);
+    std::fclose(f);
+    std::fprintf(meta, "%s %s %zu 1\n", name, dtype, rows);
+}
+
+// The dense micro-cell offset table (cells * 64 + 1 ints: 810 MB for a
+// 3.16M-cell grid) written sparsely: the index, start and count of every
+// occupied micro cell, and the total.
+static void dump_micro_sparse(const std::string &dir, const int *d_off,
+                              size_t micro_cells, FILE *meta) {
+    std::vector<int> h(micro_cells + 1);
+    CK(cudaMemcpy(h.data(), d_off, h.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    std::vector<long long> idx;
+    std::vector<int> start, count;
+    for (size_t m = 0; m < micro_cells; ++m) {
+        const int c = h[m + 1] - h[m];
+        if (c != 0) {
+            idx.push_back((long long)m);
+            start.push_back(h[m]);
+            count.push_back(c);
+        }
+    }
+    std::fprintf(meta, "micro_total %d\n", h[micro_cells]);
+    write_host(dir, "micro_index", idx.data(), idx.size() * 8, idx.size(), meta, "int64");
+    write_host(dir, "micro_start", start.data(), start.size() * 4, start.size(), meta,
+               "int32");
+    write_host(dir, "micro_count", count.data(), count.size() * 4, count.size(), meta,
+               "int32");
+}
+
 static int run_tick(const Kernels &k, const Scene &sc, const std::string &dir) {
     RefState st = make_state(sc, k);
     const float inv_cell = sc.p.inv_cell_size;
@@ -424,7 +462,7 @@ static int run_tick(const Kernels &k, const Scene &sc, const std::string &dir) {
     dump<int>(dir, "hash", st.d_hash, N, meta, "int32");
     dump<int>(dir, "cell_offset", st.d_cell_offset, C, meta, "int32");
     dump<int>(dir, "cell_nump", st.d_cell_nump, C, meta, "int32");
-    dump<int>(dir, "cell_offset_M", st.d_cell_offset_M, C * 64 + 1, meta, "int32");
+    dump_micro_sparse(dir, st.d_cell_offset_M, C * 64, meta);
     dump<int>(dir, "block_req", st.d_block_reqs, C, meta, "int32");
     dump<int>(dir, "index", st.d_index, N, meta, "int32");
     const int T = st.task_count;

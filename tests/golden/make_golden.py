@@ -63,6 +63,11 @@ def scenes(g):
     out["dense_default"] = (p, shuffled(pos, seed=22))
     s, p, pos = mixed_scene(g)
     out["mixed"] = (p, shuffled(pos, seed=23))
+    # 32^3 = 32,768 particles of the 262,144-particle dam break (64^3, seed 0):
+    # the same physics and proportions at half the size (column in the lower
+    # left quarter of a 1.28 x 0.64 x 0.64 m box)
+    s, p, pos = dam_scene(g, n_side=32, box=(1.28, 0.64, 0.64), seed=0)
+    out["dam_32k"] = (p, shuffled(pos, seed=24))
     return out
 
 
@@ -70,13 +75,7 @@ def params_bytes(p) -> np.ndarray:
     return np.frombuffer(ctypes.string_at(ctypes.addressof(p), ctypes.sizeof(p)), np.uint8)
 
 
-def micro_sparse(offsets: np.ndarray):
-    counts = np.diff(offsets.astype(np.int64))
-    idx = np.nonzero(counts)[0]
-    return idx.astype(np.int64), offsets[idx].astype(np.int32), counts[idx].astype(np.int32)
-
-
-def record(out_dir: Path):
+def record(out_dir: Path, only=None):
     from oracle import refharness as rh
     g = ge.package()
     out_dir.mkdir(parents=True, exist_ok=True)
@@ -84,15 +83,17 @@ def record(out_dir: Path):
     for name, (p, pos) in scenes(g).items():
         vel = np.zeros_like(pos)
         vel[:, :3] = rng.normal(0.0, 0.3, (len(pos), 3))
+        if only and name not in only:
+            continue   # the velocities are drawn all the same: one stream
         ev = vel.copy()
         r = rh.run_tick(p, pos, vel, ev)
-        mi, ms, mc = micro_sparse(r["cell_offset_M"])
+        mi, ms, mc = r["micro_index"], r["micro_start"], r["micro_count"]
         np.savez_compressed(
             out_dir / f"{name}.npz",
             params=params_bytes(p), in_pos=pos, in_vel=vel, in_ev=ev,
             hash=r["hash"], cell_offset=r["cell_offset"], cell_nump=r["cell_nump"],
             micro_index=mi, micro_start=ms, micro_count=mc,
-            micro_total=np.int64(r["cell_offset_M"][-1]),
+            micro_total=np.int64(r["micro_total"]),
             block_req=r["block_req"], index=r["index"],
             middle=np.int32(r["middle"]), task_count=np.int32(r["task_count"]),
             tasks=r["tasks"], sorted_pos=r["sorted_pos"], sorted_vel=r["sorted_vel"],
@@ -120,12 +121,13 @@ def main():
     ap.add_argument("--out", default=str(Path(__file__).resolve().parent))
     ap.add_argument("--bench", action="store_true")
     ap.add_argument("--frames", type=int, default=200)
+    ap.add_argument("--only", nargs="*", help="record only these scenes")
     a = ap.parse_args()
     ge.build()
     if a.bench:
         bench(a.frames)
     else:
-        record(Path(a.out))
+        record(Path(a.out), a.only)
 
 
 if __name__ == "__main__":

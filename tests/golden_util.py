@@ -14,7 +14,7 @@ from pathlib import Path
 import numpy as np
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
-SCENES = ["sparse_dam", "dense_default", "mixed"]
+SCENES = ["sparse_dam", "dense_default", "mixed", "dam_32k"]
 
 
 def load(name: str, params_cls):

@@ -2,9 +2,10 @@
 
 tests/golden/*.npz were recorded by tests/golden/make_golden.py: one frame of
 the reference's own CUDA kernels (compiled unmodified from its sources and
-driven by oracle/refharness) on three scenes — a sparse dam break (all TRA),
-the reference's default-scene physics (all SMS) and a mixed scene (TRA + SMS,
-odd task count, every performance-model branch). Integer stages must match
+driven by oracle/refharness) on four scenes — a sparse dam break (all TRA),
+the reference's default-scene physics (all SMS), a mixed scene (TRA + SMS,
+odd task count, every performance-model branch) and 32,768 particles of the
+262,144-particle dam break (its physics and proportions at half the size). Integer stages must match
 exactly (modulo the reference's run-to-run order inside a micro cell);
 physics within the stated tolerances of the FP64 oracle.
 """
