@@ -162,13 +162,14 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel: str, key: str = ""):
+def ncu_traffic(kernel: str, workload: str, key: str = ""):
     """Per-launch DRAM bytes of `kernel` (or its `.key` figure) from the
-    committed ncu summary."""
+    committed ncu summary of the same workload (`kernel@workload = value`);
+    None where no capture of this workload exists."""
     f = ROOT / "profiles" / "traffic_per_launch.txt"
     if not f.exists():
         return None
-    name = re.escape(kernel + (f".{key}" if key else ""))
+    name = re.escape(f"{kernel}@{workload}" + (f".{key}" if key else ""))
     for line in f.read_text().splitlines():
         m = re.match(rf"\s*{name}\s*=\s*([0-9.eE+]+)", line)
         if m:
@@ -218,41 +219,71 @@ def cpu_oracle_rate(params, pos, budget_s: float, max_steps: int, vel=None, ev=N
     return len(P) * steps / dt, steps, len(P), oracle.num_threads()
 
 
-def run_reference(args, ws, rank):
-    if rank != 0:
-        return 0
-    g = load_pkg()
-    s = g.load_scene(g.scene_path(SCENE))
-    p = g.params_init(s)
-    n_full = len(g.lattice(s, p))
+def reference_scene(scene_file: str):
+    """Scene, parameters and lattice of a scene file through the oracle alone
+    (its JSON reader, parameter and lattice restatements): the CPU reference
+    arm loads no part of the GPU library. The package module is imported only
+    for its ctypes struct layouts (it loads libgsph.so lazily, not here)."""
     import oracle
     oracle.build()
-    # each step: one FP64 frame on a sample sized so K + W steps take minutes
-    total = max(1, args.steps + args.warmup)
-    sample_n = int(min(n_full, max(65536, n_full * 24 // total)))
-    vel_state = None
-    pos = g.lattice(s, p)[:sample_n].copy()
-    P = np.array(pos, np.float64)
-    V = np.zeros_like(P)
-    E = np.zeros_like(P)
+    g = load_pkg()
+    path = ROOT / "fast-general-gpu-sph-framework_gb300" / "scenes" / scene_file
+    s = oracle.scene_from_json(path.read_text(), g.Scene)
+    p = oracle.params_init(s, g.Params)
+    return s, p, oracle.lattice(s, p)
+
+
+def run_reference(args, ws, rank):
+    """The reference's step on the host cores: the FP64 C/OpenMP restatement
+    of HybridSystem::tick() (the reference itself has no CPU path), one full
+    frame of the whole scene per step on all host threads. When K + W full
+    frames would take more than a few minutes, each step is instead a frame of
+    the first M particles of the lattice, M sized to fit (stated in the line)."""
+    if rank != 0:
+        return 0
+    import oracle
+    s, p, pos_full = reference_scene(args.scene)
+    n_full = len(pos_full)
     lib = oracle._load()
+
+    def state(m):
+        P = np.array(pos_full[:m], np.float64)
+        return P, np.zeros_like(P), np.zeros_like(P)
+
+    # one untimed full frame sizes the run: K + W frames within ~3 minutes
+    P, V, E = state(n_full)
+    t = time.perf_counter()
+    lib.oracle_step(P.ctypes.data, V.ctypes.data, E.ctypes.data, len(P), oracle._ref(p))
+    t_full = time.perf_counter() - t
+    total = max(1, args.steps + args.warmup)
+    budget_s = 180.0
+    sample_n = n_full if total * t_full <= budget_s else max(
+        65536, int(n_full * budget_s / (total * t_full)))
+    if sample_n < n_full:
+        P, V, E = state(sample_n)
     for _ in range(args.warmup):
         lib.oracle_step(P.ctypes.data, V.ctypes.data, E.ctypes.data, len(P), oracle._ref(p))
     t0 = time.perf_counter()
     for _ in range(args.steps):
         lib.oracle_step(P.ctypes.data, V.ctypes.data, E.ctypes.data, len(P), oracle._ref(p))
     dt = time.perf_counter() - t0
-    del vel_state
     value = sample_n * args.steps / dt
-    sample = (f"{sample_n} of {n_full} particles (first lattice slabs of the 3.94M "
-              f"column) per step, FP64 C/OpenMP restatement of the reference step")
+    if sample_n == n_full:
+        sample = (f"every step one FP64 frame of all {n_full} particles, FP64 C/OpenMP "
+                  f"restatement of the reference step")
+    else:
+        sample = (f"every step one FP64 frame of the first {sample_n} of {n_full} particles "
+                  f"(K + W full frames would exceed {budget_s:.0f} s), FP64 C/OpenMP "
+                  f"restatement of the reference step")
+    workload = WORKLOAD if args.scene == SCENE else args.scene
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "particle-steps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dt * 1e3 / max(args.steps, 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: seeded jittered dam-break lattice generated on the host",
-        "config": {"workload": WORKLOAD, "parallelism": "rank 0 only (CPU)"},
+        "config": {"workload": workload, "particles": sample_n,
+                   "parallelism": "rank 0 only (CPU)"},
         "cpu_baseline": {"value": value, "unit": "particle-steps/s",
                          "cores": oracle.num_threads(), "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
@@ -625,7 +656,10 @@ def main():
         p = g.params_init(s)
         cpu_state = (p, g.lattice(s, p), None, None,
                      "FP64 frame(s) of the full {n}-particle scene")
-    line = measure_scene(g, sysm, args, ws, rank, local, dist, workload, cpu_state)
+    capture_key = (f"stress_{args.stress_side}" if args.workload == "stress"
+                   else Path(args.scene).stem)
+    line = measure_scene(g, sysm, args, ws, rank, local, dist, workload, cpu_state,
+                         capture_key)
     if line is not None:
         print(json.dumps(line))
     dist.close()
@@ -674,7 +708,7 @@ def prepare_stress(g, args, local):
                             "restarted state")
 
 
-def measure_scene(g, sysm, args, ws, rank, local, dist, workload, cpu_state):
+def measure_scene(g, sysm, args, ws, rank, local, dist, workload, cpu_state, capture_key):
     import torch
     n = sysm.n
     stream = torch.cuda.ExternalStream(sysm.stream(), device=torch.device("cuda", local))
@@ -730,7 +764,7 @@ def measure_scene(g, sysm, args, ws, rank, local, dist, workload, cpu_state):
     info = sysm.info()
     # the stage is one TRA and one SMS launch; name the one that does the work
     kernel = f"k_{dom}_" + ("sms" if info.tra_particles == 0 else "tra")
-    traffic = ncu_traffic(kernel)
+    traffic = ncu_traffic(kernel, capture_key)
     # both passes against the same cell-tile model (each stage = its TRA and
     # SMS launches back to back)
     per_stage = {}
@@ -793,7 +827,10 @@ def measure_scene(g, sysm, args, ws, rank, local, dist, workload, cpu_state):
         "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "algorithmic_bytes": b_dom,
-                     "fp32_pipe_frac": ncu_traffic(kernel, "fma_pipe"),
+                     "traffic_source": (f"profiles/traffic_per_launch.txt, ncu capture of "
+                                        f"{capture_key}") if traffic else
+                                       "no ncu capture of this workload",
+                     "fp32_pipe_frac": ncu_traffic(kernel, capture_key, "fma_pipe"),
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
                      if peak_kind == "measured" else "fallback 6800 GB/s"},
         "roofline_stages": per_stage,

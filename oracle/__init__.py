@@ -75,6 +75,43 @@ def num_threads() -> int:
     return int(_load().oracle_num_threads())
 
 
+def scene_from_json(text, scene_cls, max_blocks: int = 64):
+    """readSceneFromJsonFile (src/simulation/sph_hybrid_system.cpp:69-126) with
+    the Scene defaults of sph_hybrid_system.h:37-44, restated on Python's json
+    reader: numbers are read as doubles and stored as floats; a missing
+    fluid_block bound reads 0 (jsoncpp's null); the optional physics keys stay
+    NaN when absent (parameter defaults apply)."""
+    import json
+    d = json.loads(text)
+    s = scene_cls()
+    nan = float("nan")
+    s.interval, s.mass, s.recomm_nump = 0.5, 0.02, 65536
+    for name in ("kernel", "rest_density", "gas_constant", "viscosity", "time_step",
+                 "gravity_y"):
+        setattr(s, name, nan)
+    s.jitter, s.seed = 0.0, 0
+    for a, k in enumerate(("xx", "yy", "zz")):
+        if k in d:
+            s.world[a] = float(d[k])
+    for k in ("mass", "interval", "kernel", "rest_density", "gas_constant", "viscosity",
+              "time_step", "gravity_y", "jitter"):
+        if k in d:
+            setattr(s, k, float(d[k]))
+    if "recomm_nump" in d:
+        s.recomm_nump = int(d["recomm_nump"])
+    if "seed" in d:
+        s.seed = int(d["seed"])
+    blocks = d.get("fluid_block", [])
+    if len(blocks) > max_blocks:
+        raise ValueError(f"scene has {len(blocks)} fluid blocks (max {max_blocks})")
+    for i, b in enumerate(blocks):
+        for a, ax in enumerate("xyz"):
+            s.block_begin[i][a] = float(b.get(f"begin_{ax}", 0.0))
+            s.block_end[i][a] = float(b.get(f"end_{ax}", 0.0))
+    s.n_blocks = len(blocks)
+    return s
+
+
 def params_init(scene, params_cls):
     """defaultInitializeSPHSysPara restated; returns a new params struct."""
     p = params_cls()

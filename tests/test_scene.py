@@ -122,3 +122,13 @@ def test_params_rejects_bad_grid(gsph):
     with pytest.raises(gsph.GsphError) as ei:
         gsph.params_init(s)
     assert ei.value.status in (gsph.ERR_INVALID_ARG, gsph.ERR_CAPACITY)
+
+
+@pytest.mark.parametrize("name", SCENES)
+def test_oracle_json_reader_matches_library(gsph, oracle, name):
+    """The oracle's own scene reader (used where the library must not be
+    loaded, e.g. the benchmark's CPU reference arm) gives the same struct."""
+    mine = gsph.load_scene(gsph.scene_path(name))
+    ref = oracle.scene_from_json(gsph.scene_path(name).read_text(), gsph.Scene)
+    assert C.string_at(C.addressof(mine), C.sizeof(mine)) == \
+        C.string_at(C.addressof(ref), C.sizeof(ref))
