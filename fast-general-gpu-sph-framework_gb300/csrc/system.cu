@@ -765,7 +765,7 @@ struct System {
         GSPH_CUDA(cudaMalloc(&saved, 3 * bytes));
         const int cur0 = cur;
         const uint64_t frames0 = frames;
-        const bool arranged0 = arranged, grid0 = grid_current;
+        const bool arranged0 = arranged;
         const int graphs0 = graph_frames;
         const bool timing0 = timing;
         auto restore = [&]() -> gsph_status {
@@ -818,7 +818,9 @@ struct System {
         set_tuning(best_k >= 0 && !st ? cand[best_k] : start);
         frames = frames0;
         arranged = arranged0;
-        grid_current = grid0;
+        // the trials' sorts rewrote the grid arrays (offsets, keys, tasks):
+        // the restored state needs a new arrange
+        grid_current = false;
         lists_valid = false;
         hashed = false;
         counts_dirty = true;

@@ -90,3 +90,25 @@ def test_autotuner_caches_by_occupancy_histogram(gsph, cuda_device):
         t2, _, cached2 = tuner.tune(h)
         assert h.get_tuning().as_dict() == t1.as_dict()
     assert not cached1 and cached2 and t1.as_dict() == t2.as_dict()
+
+
+def test_autotune_leaves_the_grid_to_be_rebuilt(gsph, oracle, cuda_device):
+    """The trials sort their own states, so after autotune the grid arrays do
+    not describe the restored state: stage calls need a new arrange (they are
+    refused until then), and after it density matches the oracle."""
+    _, p, pos = dam_scene(gsph, n_side=14, box=(0.6, 0.4, 0.4))
+    with gsph.HybridSystem(params=p, positions=shuffled(pos)) as h:
+        h.step(2)
+        h.arrange()
+        h.autotune(frames_per_trial=1)
+        with pytest.raises(gsph.GsphError) as ei:
+            h.density()
+        assert ei.value.status == gsph.ERR_STATE
+        h.arrange()
+        h.density()
+        spos = h.copy_out(gsph.FIELD_POSITION)
+        ks = h.copy_out(gsph.FIELD_KEY)
+        cs = h.copy_out(gsph.FIELD_CELL_START)
+    rho, _ = oracle.density(spos, ks, cs, p)
+    err = np.abs(1.0 / spos[:, 3].astype(np.float64) - rho) / rho
+    assert err.max() <= RHO_TOL
