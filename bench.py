@@ -12,11 +12,17 @@ L2 flush is needed), takes per-stage times from the frames that follow (stage
 events, frame by frame), samples SM clocks
 during the timed region, measures the end-to-end rate through the public API
 with pinned host buffers, reports the roofline of the dominant kernel and
-times the CPU oracle on the host cores as a reported baseline. The reference
-arm (--impl reference) times the CPU restatement of the reference's step on a
-bounded sample of the same workload (the reference has no CPU path of its
-own). With N > 1 (torchrun), every rank runs an independent replica: the
-path does not shard.
+times the CPU oracle on the host cores as a reported baseline. The same line
+carries the metric's batched and served forms as sub-records: 256 uneven
+scenes stepped as one batch (100 frames in one CUDA graph, autotuned) against
+per-scene loops of the plain path (kernel by kernel and as CUDA graphs of the
+same length), and 10 s of Poisson request arrivals through the native
+continuous-batching server against the same trace through an executed
+per-scene FIFO loop, with p50/p99 completion latency. The reference arm
+(--impl reference) times the CPU restatement of the reference's step (the
+reference has no CPU path of its own): full FP64 frames of the same scene.
+With N > 1 (torchrun), every rank runs an independent replica: the path does
+not shard.
 """
 from __future__ import annotations
 
@@ -307,29 +313,26 @@ def load_workloads():
     return mod
 
 
-def run_batched(args, ws, rank, local):
+def batched_record(g, W, args, R, rank, local, frames, graph_frames, autotune=True):
     """Batched workload: independent dam-break scenes (N log-uniform in
     [4,096, 262,144], column aspect uniform in [0.5, 2]) stepped as one batch
-    with CUDA graphs of `graph_frames` frames, against a loop over the same
-    scenes with the plain single-scene path."""
+    with CUDA graphs of `graph_frames` frames (one launch per stage for all
+    scenes, autotuned split and launch shapes), against a loop over the same
+    scenes with the plain single-scene path, launched kernel by kernel and as
+    CUDA graphs of the same length. Returns the measurements as a dict."""
     import torch
-    torch.cuda.set_device(local)
-    R = Ranks(ws)
-    g = load_pkg()
-    W = load_workloads()
     specs = W.batched_scenes(args.scenes, seed=rank)
     scenes = [W.build(g, sp) for sp in specs]
     total = sum(len(pos) for _, pos in scenes)
-    K = args.steps
     b = g.Batch(scenes, device=local)
     b.step(args.warmup)
     b.sync()
     tuned = None
-    if not args.no_autotune:
+    if autotune:
         t, ms = b.autotune(frames_per_trial=3)
         tuned = {**t.as_dict(), "trial_ms_per_frame": ms}
-    b.set_graph_mode(args.graph_frames)
-    b.step(1)
+    b.set_graph_mode(graph_frames)
+    b.step(graph_frames)          # captures the graph outside the timed region
     b.sync()
     stream = torch.cuda.ExternalStream(b.stream(), device=torch.device("cuda", local))
     ev0 = torch.cuda.Event(enable_timing=True)
@@ -341,58 +344,86 @@ def run_batched(args, ws, rank, local):
     time.sleep(0.3)
     t0 = time.perf_counter()
     ev0.record(stream)
-    b.step(K)
+    b.step(frames)
     ev1.record(stream)
     ev1.synchronize()
     wall_b = time.perf_counter() - t0
     clk = clocks.stop()
     dev_ms = ev0.elapsed_time(ev1)
+    b.set_graph_mode(0)
+    b.set_stage_timing(True)
+    b.step(10)
+    stages = b.stage_times()
     info = b.info()
     b.close()
     dev_ms = R.max(dev_ms)
     total_all = R.sum(total)
-    batched = total_all * K / (dev_ms / 1e3)
+    batched = total_all * frames / (dev_ms / 1e3)
 
-    def loop_rate(graph_frames):
+    def loop_rate(gf):
         hs = [g.HybridSystem(params=p, positions=pos, device=local) for p, pos in scenes]
         for h in hs:
-            h.set_graph_mode(graph_frames)
-            h.step(args.warmup)
+            h.set_graph_mode(gf)
+            h.step(max(args.warmup, gf))   # with graphs: the capture happens here
             h.sync()
         R.barrier()
         torch.cuda.synchronize()
         t = time.perf_counter()
         for h in hs:
-            h.step(K)
+            h.step(frames)
             h.sync()
         dt = R.max(time.perf_counter() - t)
         for h in hs:
             h.close()
-        return total_all * K / dt, dt
+        return total_all * frames / dt, dt
 
     loop_plain, t_plain = loop_rate(0)
-    loop_graph, t_graph = loop_rate(args.graph_frames)
-    line = {
-        "metric": "aggregate particle-steps/s, batched vs per-scene loop",
-        "value": batched, "unit": "particle-steps/s", "n_gpus": ws, "steps": K,
-        "warmup": args.warmup, "ms_per_step": dev_ms / K, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic: seeded jittered dam-break columns generated on the host",
-        "config": {"workload": f"batched: {len(scenes)} scenes per GPU, {total} particles, "
-                               f"N log-uniform [4096, 262144], aspect U[0.5, 2], "
-                               f"262k-scene physics, own boxes",
-                   "graph_frames": args.graph_frames, "cells": int(info.n_cells),
-                   "tuning": tuned if tuned else "reference thresholds, default shapes"},
-        "batched_wall_s": wall_b,
+    loop_graph, t_graph = loop_rate(graph_frames)
+    return {
+        "value": batched, "unit": "particle-steps/s", "frames": frames,
+        "ms_per_frame": dev_ms / frames, "wall_s": wall_b,
+        "workload": f"{len(scenes)} scenes per GPU, {total} particles, N log-uniform "
+                    f"[4096, 262144], aspect U[0.5, 2], 262k-scene physics, own boxes",
+        "scenes": len(scenes), "particles": total, "cells": int(info.n_cells),
+        "graph_frames": graph_frames,
+        "timing": f"CUDA events around {frames} frames launched as CUDA graphs of "
+                  f"{graph_frames} frames; stage times from 10 frames that follow",
+        "tuning": tuned if tuned else "reference thresholds, default shapes",
+        "split": {"tra_particles": info.tra_particles, "sms_tasks": info.sms_tasks},
+        "stages_ms": stages,
         "per_scene_loop": {"value": loop_plain, "unit": "particle-steps/s",
                            "wall_s": t_plain, "launch": "kernel by kernel"},
         "per_scene_loop_graphs": {"value": loop_graph, "unit": "particle-steps/s",
                                   "wall_s": t_graph,
-                                  "launch": f"CUDA graphs of {args.graph_frames} frames"},
+                                  "launch": f"CUDA graphs of {graph_frames} frames"},
         "speedup_vs_loop": batched / loop_plain,
         "speedup_vs_graph_loop": batched / loop_graph,
         "clocks": clk,
-        "gpu_launches": LAUNCHES_PER_FRAME * K,
+        "gpu_launches": LAUNCHES_PER_FRAME * frames,
+    }
+
+
+def run_batched(args, ws, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    R = Ranks(ws)
+    g = load_pkg()
+    W = load_workloads()
+    rec = batched_record(g, W, args, R, rank, local, args.steps, args.graph_frames,
+                         autotune=not args.no_autotune)
+    line = {
+        "metric": "aggregate particle-steps/s, batched vs per-scene loop",
+        "value": rec["value"], "unit": "particle-steps/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": rec["ms_per_frame"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded jittered dam-break columns generated on the host",
+        "config": {"workload": "batched: " + rec["workload"],
+                   "graph_frames": args.graph_frames, "cells": rec["cells"],
+                   "tuning": rec["tuning"]},
+        **{k: rec[k] for k in ("stages_ms", "split", "per_scene_loop",
+                               "per_scene_loop_graphs", "speedup_vs_loop",
+                               "speedup_vs_graph_loop", "clocks", "gpu_launches")},
+        "batched_wall_s": rec["wall_s"],
     }
     if rank == 0:
         print(json.dumps(line))
@@ -414,64 +445,66 @@ def load_serve():
     return mod
 
 
-def fifo_loop_model(g, W, trace, local, warmup):
-    """Per-scene FIFO loop of the plain path over the same trace: the frame
-    time of a single scene is measured at log-spaced sizes across the trace's
-    range (stream launches, state resident), interpolated in log-log for each
-    request, and the FIFO queue is replayed with service = K x frame time."""
-    sizes = sorted({(sp["nx"], sp["ny"], sp["nz"]) for _, sp, _ in trace},
-                   key=lambda s: s[0] * s[1] * s[2])
-    picks = [sizes[int(round(q * (len(sizes) - 1)))] for q in np.linspace(0, 1, 8)]
-    pts = []
-    for nx, ny, nz in dict.fromkeys(picks):
-        p, pos = W.build(g, {"nx": nx, "ny": ny, "nz": nz, "seed": 5})
-        with g.HybridSystem(params=p, positions=pos, device=local) as h:
-            h.step(warmup)
-            h.sync()
-            frames = max(10, min(200, int(2e8 / max(len(pos), 1))))
-            t = time.perf_counter()
-            h.step(frames)
-            h.sync()
-            pts.append((len(pos), (time.perf_counter() - t) / frames))
-    ln = np.log([n for n, _ in pts])
-    lt = np.log([t for _, t in pts])
-
-    def frame_s(n):
-        return float(np.exp(np.interp(np.log(n), ln, lt)))
-
-    free_at, lat, work = 0.0, [], 0.0
-    for t_arr, sp, k in trace:
-        n = sp["nx"] * sp["ny"] * sp["nz"]
-        start = max(free_at, t_arr)
-        free_at = start + k * frame_s(n)
-        lat.append(free_at - t_arr)
-        work += n * k
-    lat = np.array(lat)
-    return {"value": work / free_at, "unit": "particle-steps/s",
-            "p50_ms": float(np.percentile(lat, 50) * 1e3),
-            "p99_ms": float(np.percentile(lat, 99) * 1e3),
-            "makespan_s": free_at,
-            "frame_ms_at": {str(n): t * 1e3 for n, t in pts},
-            "method": "FIFO replay of the trace with service = K x measured "
-                      "single-scene frame time (8 sizes, log-log interpolation)"}
+def _builder(g, W, trace, ahead=16):
+    """Yields (index, params, positions) of the trace's scenes in order,
+    built by a small thread pool up to `ahead` requests in advance (the
+    lattice fill releases the GIL)."""
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=4) as pool:
+        q = collections.deque()
+        nxt = 0
+        for i in range(len(trace)):
+            while nxt < len(trace) and nxt < i + ahead:
+                q.append(pool.submit(W.build, g, trace[nxt][1]))
+                nxt += 1
+            p, pos = q.popleft().result()
+            yield i, p, pos
 
 
-def run_served(args, ws, rank, local):
+def fifo_loop_executed(g, W, S, trace, local, graph_frames):
+    """The per-scene FIFO loop of the plain single-scene path, executed: the
+    requests are served one at a time in arrival order (a request that has not
+    arrived yet is waited for), each on its own HybridSystem stepped its K
+    frames as CUDA graphs of `graph_frames` frames, with its positions read
+    back at the end. Lattices are built ahead by a thread pool (they are the
+    request's input, as in the served run)."""
+    from types import SimpleNamespace
+    done = []
+    work = 0
+    t0 = time.perf_counter()
+    for i, p, pos in _builder(g, W, trace):
+        t_arr, sp, k = trace[i]
+        wait = t_arr - (time.perf_counter() - t0)
+        if wait > 0:
+            time.sleep(wait)
+        h = g.HybridSystem(params=p, positions=pos, device=local)
+        h.set_graph_mode(graph_frames)
+        h.step(k)
+        h.copy_out(g.FIELD_POSITION)     # result read-back (synchronises)
+        h.close()
+        done.append(SimpleNamespace(rid=i, t_arrival=t0 + t_arr,
+                                    t_done=time.perf_counter()))
+        work += len(pos) * k
+    makespan = time.perf_counter() - t0
+    lat = S.latency_stats(done)
+    return {"value": work / makespan, "unit": "particle-steps/s", "latency": lat,
+            "makespan_s": makespan, "requests": len(done),
+            "method": f"executed: one request at a time in arrival order, each its own "
+                      f"HybridSystem stepped K frames as CUDA graphs of {graph_frames} "
+                      f"frames, positions read back"}
+
+
+def served_record(g, W, S, args, R, rank, local, duration):
     """Served workload: Poisson arrivals (50/s) of dam-break requests (N
     log-uniform in [8,192, 1,048,576], K uniform in [50, 500]) replayed in
-    real time. A client thread builds each scene when it arrives; the server
-    admits queued requests FIFO between chunks of frames while they fit the
-    HBM budget and the batch's capacity, steps all resident scenes together
-    and retires each after its K frames (its positions are read back)."""
-    import torch
-    torch.cuda.set_device(local)
-    R = Ranks(ws)
-    g = load_pkg()
-    W = load_workloads()
-    S = load_serve()
-    trace = W.served_requests(args.duration, seed=1 + rank)
+    real time for `duration` seconds of arrivals. A client thread builds each
+    scene when it arrives; the server admits queued requests FIFO between
+    chunks of frames while they fit the HBM budget and the batch's capacity,
+    steps all resident scenes together and retires each after its K frames
+    (its positions are read back). Then the same trace through the executed
+    per-scene FIFO loop. Returns the measurements as a dict."""
+    trace = W.served_requests(duration, seed=1 + rank)
     budget = int(args.budget_gb * 1e9)
-    # the batch's key space holds 2^26 global cells; particles sized to match
     cap = (args.cap_particles, (1 << 26) - 1, 4096)
     native = args.server == "native"
     if native:
@@ -492,31 +525,18 @@ def run_served(args, ws, rank, local):
     errors = []
 
     def client():
-        # scenes are built up to 2 s ahead of their arrival by a small pool
-        # (the lattice fill releases the GIL) and submitted at arrival time
-        from concurrent.futures import ThreadPoolExecutor
-        ahead = collections.deque()
-        nxt = 0
+        # scenes are built ahead of their arrival and submitted at arrival time
         try:
-            with ThreadPoolExecutor(max_workers=4) as pool:
-                for i, (t_arr, sp, k) in enumerate(trace):
-                    while nxt < len(trace) and trace[nxt][0] <= (
-                            time.perf_counter() - t0) + 2.0:
-                        ahead.append(pool.submit(W.build, g, trace[nxt][1]))
-                        nxt += 1
-                    if not ahead:
-                        ahead.append(pool.submit(W.build, g, sp))
-                        nxt += 1
-                    fut = ahead.popleft()
-                    dt = t0 + t_arr - time.perf_counter()
-                    if dt > 0:
-                        time.sleep(dt)
-                    p, pos = fut.result()
-                    if native:
-                        arrivals[i] = (t0 + t_arr, len(pos), k)
-                        srv.submit(i, p, pos, k)
-                    else:
-                        srv.submit(S.Request(i, p, pos, k, t0 + t_arr))
+            for i, p, pos in _builder(g, W, trace):
+                t_arr, sp, k = trace[i]
+                dt = t0 + t_arr - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                if native:
+                    arrivals[i] = (t0 + t_arr, len(pos), k)
+                    srv.submit(i, p, pos, k)
+                else:
+                    srv.submit(S.Request(i, p, pos, k, t0 + t_arr))
         except Exception as e:         # surfaced after the run
             errors.append(e)
         finally:
@@ -578,30 +598,52 @@ def run_served(args, ws, rank, local):
     served = R.sum(psteps) / makespan
     lat = S.latency_stats(done)
     offered = sum(sp["nx"] * sp["ny"] * sp["nz"] * k for _, sp, k in trace)
-    loop = fifo_loop_model(g, W, trace, local, args.warmup)
-    line = {
-        "metric": "served aggregate particle-steps/s with p50/p99 completion latency",
-        "value": served, "unit": "particle-steps/s", "n_gpus": ws, "steps": frames,
-        "warmup": args.warmup, "ms_per_step": busy * 1e3 / max(frames, 1),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic: seeded Poisson trace of jittered dam-break columns, "
-                "lattices built on arrival",
-        "config": {"workload": f"served: {len(trace)} requests over {args.duration:g} s "
-                               f"(Poisson 50/s), N log-uniform [8192, 1048576], "
-                               f"K uniform [50, 500]",
-                   "budget_gb": args.budget_gb, "capacity_particles": cap[0],
-                   "capacity_cells": cap[1], "chunk_frames": args.chunk,
-                   "server": "native gsph_server_*" if native else "Python SceneServer"},
-        "latency": lat,
-        "requests": len(done), "offered_particle_steps": offered,
-        "makespan_s": makespan, "server_busy_s": busy,
-        "host_s": host_s,
-        "rejected": rejected,
+    loop = fifo_loop_executed(g, W, S, trace, local, args.graph_frames)
+    loop["value"] = R.sum(loop["value"])
+    return {
+        "value": served, "unit": "particle-steps/s",
+        "workload": f"{len(trace)} requests over {duration:g} s (Poisson 50/s), "
+                    f"N log-uniform [8192, 1048576], K uniform [50, 500]",
+        "latency": lat, "requests": len(done), "frames": frames, "chunks": chunks,
+        "offered_particle_steps": offered, "makespan_s": makespan,
+        "server_busy_s": busy, "ms_per_frame": busy * 1e3 / max(frames, 1),
+        "host_s": host_s, "rejected": rejected,
+        "budget_gb": args.budget_gb, "capacity_particles": cap[0],
+        "capacity_cells": cap[1], "chunk_frames": args.chunk,
+        "server": "native gsph_server_*" if native else "Python SceneServer",
         "peak_resident_scenes": peak_resident, "peak_resident_particles": peak_particles,
         "per_scene_fifo_loop": loop,
         "speedup_vs_loop": served / loop["value"],
+        "p50_vs_loop": lat["p50_ms"] / loop["latency"]["p50_ms"],
+        "p99_vs_loop": lat["p99_ms"] / loop["latency"]["p99_ms"],
         "clocks": clk,
         "gpu_launches": LAUNCHES_PER_FRAME * frames + chunks,
+    }
+
+
+def run_served(args, ws, rank, local):
+    import torch
+    torch.cuda.set_device(local)
+    R = Ranks(ws)
+    g = load_pkg()
+    W = load_workloads()
+    S = load_serve()
+    rec = served_record(g, W, S, args, R, rank, local, args.duration)
+    line = {
+        "metric": "served aggregate particle-steps/s with p50/p99 completion latency",
+        "value": rec["value"], "unit": "particle-steps/s", "n_gpus": ws,
+        "steps": rec["frames"], "warmup": args.warmup, "ms_per_step": rec["ms_per_frame"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded Poisson trace of jittered dam-break columns, "
+                "lattices built on arrival",
+        "config": {"workload": "served: " + rec["workload"],
+                   **{k: rec[k] for k in ("budget_gb", "capacity_particles",
+                                          "capacity_cells", "chunk_frames", "server")}},
+        **{k: rec[k] for k in ("latency", "requests", "offered_particle_steps",
+                               "makespan_s", "server_busy_s", "host_s", "rejected",
+                               "peak_resident_scenes", "peak_resident_particles",
+                               "per_scene_fifo_loop", "speedup_vs_loop", "p50_vs_loop",
+                               "p99_vs_loop", "clocks", "gpu_launches")},
     }
     if rank == 0:
         print(json.dumps(line))
@@ -631,6 +673,16 @@ def main():
     ap.add_argument("--chunk", type=int, default=10, help="served: frames between admissions")
     ap.add_argument("--server", default="native", choices=["native", "python"],
                     help="served: the C++ server (gsph_server_*) or the Python SceneServer")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="single: leave the batched sub-record out of the line")
+    ap.add_argument("--no-served", action="store_true",
+                    help="single: leave the served sub-record out of the line")
+    ap.add_argument("--batched-frames", type=int, default=100,
+                    help="single: timed frames of the batched sub-record")
+    ap.add_argument("--batched-graph-frames", type=int, default=100,
+                    help="single: frames per CUDA graph in the batched sub-record")
+    ap.add_argument("--served-duration", type=float, default=10.0,
+                    help="single: seconds of arrivals in the served sub-record")
     ap.add_argument("--stress-side", type=int, default=256, help="stress: column side")
     ap.add_argument("--restart-frames", type=int, default=2000,
                     help="stress: frames before the snapshot")
@@ -660,7 +712,20 @@ def main():
                    else Path(args.scene).stem)
     line = measure_scene(g, sysm, args, ws, rank, local, dist, workload, cpu_state,
                          capture_key)
+    # the batched and served forms of the same metric, on the same GPU(s)
+    extra = {}
+    if args.workload == "single":
+        W = load_workloads()
+        if not args.no_batched:
+            extra["batched"] = batched_record(g, W, args, dist, rank, local,
+                                              args.batched_frames, args.batched_graph_frames)
+        if not args.no_served:
+            extra["served"] = served_record(g, W, load_serve(), args, dist, rank, local,
+                                            args.served_duration)
     if line is not None:
+        line.update(extra)
+        if extra:
+            line["gpu_launches_sub_records"] = {k: v["gpu_launches"] for k, v in extra.items()}
         print(json.dumps(line))
     dist.close()
     return 0
