@@ -307,11 +307,56 @@ __global__ void __launch_bounds__(256) k_sort_small(Frame f) {
     }
 }
 
+// Buckets of the block-level sort past kBigCellSmem particles: 64 micro
+// cells x kSrcBuckets source-index ranges; counts and starts fit in the
+// shared staging array.
+constexpr int kSrcBuckets = 32;
+constexpr int kBuckets = 64 * kSrcBuckets;
+static_assert((2 * kBuckets + 1) * sizeof(int) <= kBigCellSmem * sizeof(unsigned long long),
+              "bucket tables must fit in the staging array");
+
+// Exclusive scan of in[0, n) into out[0, n] (out[n] = total) by the whole
+// block (blockDim.x = 256, n a multiple of 256). Ends with __syncthreads.
+__device__ void block_exclusive_scan(const int *in, int *out, int n) {
+    __shared__ int warp_sum[8];
+    __shared__ int carry;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int per = n / blockDim.x;          // items per thread, contiguous
+    const int first = threadIdx.x * per;
+    int sum = 0;
+    for (int q = 0; q < per; ++q) sum += in[first + q];
+    int x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sum[warp] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int w = 0; w < int(blockDim.x >> 5); ++w) {
+            const int v = warp_sum[w];
+            warp_sum[w] = run;
+            run += v;
+        }
+        carry = run;
+    }
+    __syncthreads();
+    int run = warp_sum[warp] + x - sum;
+    for (int q = 0; q < per; ++q) {
+        out[first + q] = run;
+        run += in[first + q];
+    }
+    if (threadIdx.x == 0) out[n] = carry;
+    __syncthreads();
+}
+
 // Cells with more than kSmallCellMax particles: one CTA per cell. Pairs
 // compare as (micro cell, source index) inside a cell, so up to kBigCellSmem
 // particles the pairs are staged in shared memory, bucketed by their 6-bit
 // micro cell (counts, scan, scatter) and ranked by value inside their bucket
-// only. Larger cells rank by counting over the whole cell in global memory.
+// only. Larger cells do the same in global memory with finer buckets.
 __global__ void __launch_bounds__(256) k_sort_big(Frame f) {
     __shared__ unsigned long long sp[kBigCellSmem];
     __shared__ uint16_t order[kBigCellSmem];
@@ -372,13 +417,43 @@ __global__ void __launch_bounds__(256) k_sort_big(Frame f) {
             __syncthreads();
             continue;
         }
+        // Past kBigCellSmem particles: bucket the cell's pairs by (micro
+        // cell, source index scaled into kSrcBuckets ranges) — an order-
+        // preserving bucket of (micro key, source) — with counts and a scan in
+        // shared memory (over the staging array) and the bucketed order in
+        // the cell's own range of f.slot (free during the sort: the hash that
+        // fills it ran before the scatter), then rank each pair inside its
+        // bucket only.
         if (threadIdx.x < 16) grp[threadIdx.x] = 0;
+        int *bcount = reinterpret_cast<int *>(sp);          // [kBuckets]
+        int *bstart = bcount + kBuckets;                     // [kBuckets + 1]
+        for (int k = threadIdx.x; k < kBuckets; k += blockDim.x) bcount[k] = 0;
         __syncthreads();
         const unsigned long long *src = f.pairs + b;
+        const unsigned long long nsrc = (unsigned long long)f.n;
+        auto bucket_of = [&](unsigned long long e) {
+            const int micro = int((e >> 32) & 63ull);
+            const int sub = int(((e & 0xFFFFFFFFull) * kSrcBuckets) / nsrc);
+            return micro * kSrcBuckets + sub;
+        };
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x)
+            atomicAdd(&bcount[bucket_of(src[i])], 1);
+        __syncthreads();
+        block_exclusive_scan(bcount, bstart, kBuckets);   // bstart[kBuckets] = cnt
+        for (int k = threadIdx.x; k < kBuckets; k += blockDim.x) bcount[k] = 0;
+        __syncthreads();
+        uint32_t *order_g = f.slot + b;
         for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-            const unsigned long long e = src[i];
-            int rank = 0;
-            for (int j = 0; j < cnt; ++j) rank += (src[j] < e) ? 1 : 0;
+            const int k = bucket_of(src[i]);
+            order_g[bstart[k] + atomicAdd(&bcount[k], 1)] = uint32_t(i);
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+            const unsigned long long e = src[order_g[t]];
+            const int k = bucket_of(e);
+            int rank = bstart[k];
+            for (int q = bstart[k]; q < bstart[k + 1]; ++q)
+                rank += (src[order_g[q]] < e) ? 1 : 0;
             move_particle(f, b + rank, e);
             atomicAdd(&grp[int((e >> 34) & 15ull)], 1);
         }

@@ -394,3 +394,31 @@ def test_render_buffers(gsph, cuda_device):
             assert np.all(r[idx] == 0) and np.all(np.abs(g[idx].astype(int) - c[idx]) <= 1)
         else:
             assert np.all(b[idx] == 0) and np.all(np.abs(r[idx].astype(int) - c[idx]) <= 1)
+
+
+@pytest.mark.parametrize("count,span", [(5000, 1.0), (70000, 1.0), (20000, 0.24)])
+def test_big_cell_sort_bit_exact(gsph, oracle, cuda_device, count, span):
+    """Cells past the shared-memory sort (4,096 particles) are bucketed by
+    (micro cell, source range) in global memory: keys, permutation and
+    offsets must still equal the oracle's stable sort — for a crowded coarse
+    cell and for one where every particle sits in a single micro cell
+    (span 0.24 of h)."""
+    s, p, base = dam_scene(gsph, n_side=8)
+    rng = np.random.default_rng(count)
+    h = float(p.kernel)
+    crowd = np.zeros((count, 4), np.float32)
+    crowd[:, :3] = 0.3002 + rng.uniform(0.0, h * span * 0.95, (count, 3))
+    pos = shuffled(np.concatenate([base, crowd]), seed=count)
+    with make(gsph, p, pos) as sysm:
+        sysm.arrange()
+        key = sysm.copy_out(gsph.FIELD_KEY)
+        perm = sysm.copy_out(gsph.FIELD_PERMUTATION)
+        cs = sysm.copy_out(gsph.FIELD_CELL_START)
+        spos = sysm.copy_out(gsph.FIELD_POSITION)
+    ks, operm, ocs, bad = oracle.sort(pos, p)
+    assert not bad
+    assert np.diff(ocs).max() >= count
+    assert np.array_equal(key, ks)
+    assert np.array_equal(perm, operm)
+    assert np.array_equal(cs, ocs)
+    assert np.array_equal(spos.view(np.uint32), pos[operm].view(np.uint32))
