@@ -52,6 +52,10 @@ FIELD_COLOR = 13
 FIELD_FINAL_POSITION = 14
 FIELD_NEIGHBOR_COUNT = 15
 
+# gsph_viscosity_model
+VISCOSITY_LAPLACIAN = 0
+VISCOSITY_ARTIFICIAL = 1
+
 
 class GsphError(RuntimeError):
     def __init__(self, status: int, message: str):
@@ -239,6 +243,7 @@ _SIGS = {
     "gsph_set_render_transform": ([_VP, C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int),
     "gsph_get_tuning": ([_VP, C.POINTER(Tuning)], C.c_int),
     "gsph_set_tuning": ([_VP, C.POINTER(Tuning)], C.c_int),
+    "gsph_set_viscosity_model": ([_VP, C.c_int, C.c_float, C.c_float], C.c_int),
     "gsph_autotune": ([_VP, C.c_int, C.POINTER(Tuning), C.c_int, C.POINTER(Tuning),
                        C.POINTER(C.c_float)], C.c_int),
     "gsph_reductions": ([_VP, C.POINTER(C.c_double)], C.c_int),
@@ -488,6 +493,13 @@ class HybridSystem:
         r = (C.c_float * 3)(*ratio)
         o = (C.c_float * 3)(*origin)
         _check(self._lib.gsph_set_render_transform(self._h, r, o))
+
+    def set_viscosity_model(self, model: int, alpha: float = 0.0, c0: float = 0.0) -> None:
+        """VISCOSITY_LAPLACIAN (the reference's, the default) or
+        VISCOSITY_ARTIFICIAL (Monaghan's artificial viscosity with alpha and
+        the speed of sound c0) for every scene of this handle."""
+        _check(self._lib.gsph_set_viscosity_model(self._h, int(model), float(alpha),
+                                                  float(c0)))
 
     def get_tuning(self) -> Tuning:
         t = Tuning()

@@ -63,6 +63,11 @@ struct DevParams {
     float gx_acc, gy_acc, gz_acc;                 // gravity
     float bmin;                                   // lower wall (= h) on every axis
     int sparse_total, sparse_self, mid_total;     // split thresholds (gsph_tuning)
+    // Artificial viscosity (GSPH_VISCOSITY_ARTIFICIAL): visc_artificial set,
+    // art_coef = alpha * c0, art_eps = 0.01 h^2, spiky = the spiky gradient
+    // constant. Unused by the reference's Laplacian model.
+    int visc_artificial;
+    float art_coef, art_eps, spiky;
 };
 
 // Geometry of one scene of a batch. Particles of scene s occupy

@@ -107,10 +107,27 @@ struct ForceAcc {
     float lap;          // colour laplacian
 };
 
+// Monaghan's artificial viscosity of one interacting pair (the optional
+// GSPH_VISCOSITY_ARTIFICIAL model, Monaghan 1992): for v_ij . r_ij < 0,
+// mu = h v_ij . r_ij / (r^2 + 0.01 h^2), Pi = -alpha c0 mu / rho_mean with
+// rho_mean = (rho_i + rho_j) / 2 = (V_i + V_j) / (2 V_i V_j), V = 1/rho.
+// Returns Pi (h - r)^2 / r, the factor of r_ij in sum_j Pi grad W / spiky;
+// zero for a separating pair.
+__device__ __forceinline__ float artificial_pair(float vr, float d2, float k,
+                                                 float inv_d, float vi, float vj,
+                                                 const DevParams &P) {
+    if (!(vr < 0.f)) return 0.f;
+    const float mu = __fdividef(P.h * vr, d2 + P.art_eps);
+    const float pij = __fdividef(-2.f * P.art_coef * mu * vi * vj, vi + vj);
+    return pij * k * k * inv_d;
+}
+
 // kChecked = false for neighbours taken from the density pass's masks: the
 // masks were set by the same squared distance and the same cut-off test, so
-// the test would always pass.
-template <bool kChecked = true>
+// the test would always pass. kArt: the viscosity slots of the accumulator
+// hold Monaghan's sum_j Pi (h - r)^2 / r r_ij instead of the reference's
+// Laplacian term.
+template <bool kChecked = true, bool kArt = false>
 __device__ __forceinline__ void force_pair(const float4 &self,
                                            const float4 &sev, const float4 &q,
                                            const float4 &qev,
@@ -128,9 +145,17 @@ __device__ __forceinline__ void force_pair(const float4 &self,
     a.px -= rx * ps;
     a.py -= ry * ps;
     a.pz -= rz * ps;
-    a.vx += (qev.x - sev.x) * wk;
-    a.vy += (qev.y - sev.y) * wk;
-    a.vz += (qev.z - sev.z) * wk;
+    if (kArt) {
+        const float vr = (sev.x - qev.x) * rx + (sev.y - qev.y) * ry + (sev.z - qev.z) * rz;
+        const float w = artificial_pair(vr, d2, k, inv_d, self.w, V, P);
+        a.vx += rx * w;
+        a.vy += ry * w;
+        a.vz += rz * w;
+    } else {
+        a.vx += (qev.x - sev.x) * wk;
+        a.vy += (qev.y - sev.y) * wk;
+        a.vz += (qev.z - sev.z) * wk;
+    }
     const float h2r2 = P.h2 - d2;
     const float wh = V * h2r2;
     const float gw = wh * h2r2;
@@ -218,9 +243,18 @@ __device__ __forceinline__ void write_force(const Frame &f, const DevParams &P,
                                             int self, const float4 &p,
                                             const float4 &pev, const SceneGeom &G,
                                             const ForceAcc &a, bool sms) {
-    float tx = a.px * P.half_spiky + a.vx * P.visco_coef;
-    float ty = a.py * P.half_spiky + a.vy * P.visco_coef;
-    float tz = a.pz * P.half_spiky + a.vz * P.visco_coef;
+    float tx, ty, tz;
+    if (P.visc_artificial) {
+        // -m rho_i sum Pi grad W: the mass is applied below with the rest
+        const float c = -P.spiky * __fdividef(1.0f, p.w);
+        tx = a.px * P.half_spiky + a.vx * c;
+        ty = a.py * P.half_spiky + a.vy * c;
+        tz = a.pz * P.half_spiky + a.vz * c;
+    } else {
+        tx = a.px * P.half_spiky + a.vx * P.visco_coef;
+        ty = a.py * P.half_spiky + a.vy * P.visco_coef;
+        tz = a.pz * P.half_spiky + a.vz * P.visco_coef;
+    }
     const float gx = a.gx * P.grad_color_scale;
     const float gy = a.gy * P.grad_color_scale;
     const float gz = a.gz * P.grad_color_scale;
@@ -521,6 +555,7 @@ k_density_sms(Frame f, DevParams P) {
 // mask) pairs in shared memory and walks all its neighbours in one loop, so
 // lanes stay converged across rows. Without masks (or with a row longer than
 // 32 candidates) the lane scans its candidates as the reference does.
+template <bool kArt>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, 4)
 k_force_tra(Frame f, DevParams P, bool fresh) {
     __shared__ uint32_t row_mask[9][kWarpsPerBlock * 32];
@@ -579,8 +614,8 @@ k_force_tra(Frame f, DevParams P, bool fresh) {
                 mask &= mask - 1u;
                 const float4 q0 = f.pos[j0], e0 = f.ev[j0];
                 const float4 q1 = f.pos[j1], e1 = f.ev[j1];
-                force_pair<false>(p, pev, q0, e0, P, a);
-                force_pair<false>(p, pev, q1, e1, P, a);
+                force_pair<false, kArt>(p, pev, q0, e0, P, a);
+                force_pair<false, kArt>(p, pev, q1, e1, P, a);
             }
             if (k < found) {
                 while (!mask) {
@@ -589,7 +624,7 @@ k_force_tra(Frame f, DevParams P, bool fresh) {
                     base = row_start[r][threadIdx.x];
                 }
                 const int j = base + __ffs(mask) - 1;
-                force_pair<false>(p, pev, f.pos[j], f.ev[j], P, a);
+                force_pair<false, kArt>(p, pev, f.pos[j], f.ev[j], P, a);
             }
         } else {
             for (int r = 0; r < 9; ++r) {
@@ -604,7 +639,7 @@ k_force_tra(Frame f, DevParams P, bool fresh) {
                     const float rx = p.x - q.x, ry = p.y - q.y, rz = p.z - q.z;
                     const float d2 = sq_dist(rx, ry, rz);
                     if (P.h2 < d2 || kFloatSmall > d2) continue;
-                    force_pair(p, pev, q, f.ev[j], P, a);
+                    force_pair<true, kArt>(p, pev, q, f.ev[j], P, a);
                 }
             }
         }
@@ -622,6 +657,7 @@ k_force_tra(Frame f, DevParams P, bool fresh) {
 // skipped when no lane of the warp interacts with either candidate. Each
 // term rounds as the reference's scalar expression; the two halves of every
 // accumulator are summed at the end.
+template <bool kArt>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, 4)
 k_force_sms(Frame f, DevParams P) {
     // candidate pair k (slots 2k, 2k+1) as four float4s: (x, x, y, y),
@@ -731,9 +767,28 @@ k_force_sms(Frame f, DevParams P) {
                         Px = __ffma2_rn(dx, ps, Px);
                         Py = __ffma2_rn(dy, ps, Py);
                         Pz = __ffma2_rn(dz, ps, Pz);
-                        Vx = __ffma2_rn(__fadd2_rn(make_float2(qc.x, qc.y), nvx), wk, Vx);
-                        Vy = __ffma2_rn(__fadd2_rn(make_float2(qc.z, qc.w), nvy), wk, Vy);
-                        Vz = __ffma2_rn(__fadd2_rn(make_float2(qd.x, qd.y), nvz), wk, Vz);
+                        const float2 dvx = __fadd2_rn(make_float2(qc.x, qc.y), nvx);
+                        const float2 dvy = __fadd2_rn(make_float2(qc.z, qc.w), nvy);
+                        const float2 dvz = __fadd2_rn(make_float2(qd.x, qd.y), nvz);
+                        if (kArt) {
+                            // v_ij . r_ij = (v_j - v_i) . (x_j - x_i); the sum is
+                            // kept against d = x_j - x_i and negated at the end
+                            float2 vr = __fmul2_rn(dvx, dx);
+                            vr = __ffma2_rn(dvy, dy, vr);
+                            vr = __ffma2_rn(dvz, dz, vr);
+                            const float2 w = make_float2(
+                                okx ? artificial_pair(vr.x, d2s.x, kk.x, inv.x, p.w, qb.z, P)
+                                    : 0.f,
+                                oky ? artificial_pair(vr.y, d2s.y, kk.y, inv.y, p.w, qb.w, P)
+                                    : 0.f);
+                            Vx = __ffma2_rn(dx, w, Vx);
+                            Vy = __ffma2_rn(dy, w, Vy);
+                            Vz = __ffma2_rn(dz, w, Vz);
+                        } else {
+                            Vx = __ffma2_rn(dvx, wk, Vx);
+                            Vy = __ffma2_rn(dvy, wk, Vy);
+                            Vz = __ffma2_rn(dvz, wk, Vz);
+                        }
                         const float2 wh = __fmul2_rn(V, t);
                         const float2 gw = __fmul2_rn(wh, t);
                         Gx = __ffma2_rn(dx, gw, Gx);
@@ -750,9 +805,9 @@ k_force_sms(Frame f, DevParams P) {
             a.px = Px.x + Px.y;
             a.py = Py.x + Py.y;
             a.pz = Pz.x + Pz.y;
-            a.vx = Vx.x + Vx.y;
-            a.vy = Vy.x + Vy.y;
-            a.vz = Vz.x + Vz.y;
+            a.vx = kArt ? -(Vx.x + Vx.y) : Vx.x + Vx.y;
+            a.vy = kArt ? -(Vy.x + Vy.y) : Vy.x + Vy.y;
+            a.vz = kArt ? -(Vz.x + Vz.y) : Vz.x + Vz.y;
             a.gx = -(Gx.x + Gx.y);
             a.gy = -(Gy.x + Gy.y);
             a.gz = -(Gz.x + Gz.y);
@@ -935,8 +990,10 @@ cudaError_t configure_physics_kernels(int device) {
     if (e != cudaSuccess) return e;
     if ((e = set_carveout(k_density_tra, kMaxShape.density_tra, smem))) return e;
     if ((e = set_carveout(k_density_sms, kMaxShape.density_sms, smem))) return e;
-    if ((e = set_carveout(k_force_tra, kMaxShape.force_tra, smem))) return e;
-    return set_carveout(k_force_sms, kMaxShape.force_sms, smem);
+    if ((e = set_carveout(k_force_tra<false>, kMaxShape.force_tra, smem))) return e;
+    if ((e = set_carveout(k_force_tra<true>, kMaxShape.force_tra, smem))) return e;
+    if ((e = set_carveout(k_force_sms<false>, kMaxShape.force_sms, smem))) return e;
+    return set_carveout(k_force_sms<true>, kMaxShape.force_sms, smem);
 }
 
 void launch_density(const Frame &f, const DevParams &P, int num_sms,
@@ -949,8 +1006,13 @@ void launch_density(const Frame &f, const DevParams &P, int num_sms,
 void launch_force(const Frame &f, const DevParams &P, int num_sms, bool fresh,
                   const LaunchShape &shape, cudaStream_t s) {
     if (f.n <= 0) return;
-    k_force_tra<<<num_sms * shape.force_tra, kWarpsPerBlock * 32, 0, s>>>(f, P, fresh);
-    k_force_sms<<<num_sms * shape.force_sms, kWarpsPerBlock * 32, 0, s>>>(f, P);
+    if (P.visc_artificial) {
+        k_force_tra<true><<<num_sms * shape.force_tra, kWarpsPerBlock * 32, 0, s>>>(f, P, fresh);
+        k_force_sms<true><<<num_sms * shape.force_sms, kWarpsPerBlock * 32, 0, s>>>(f, P);
+    } else {
+        k_force_tra<false><<<num_sms * shape.force_tra, kWarpsPerBlock * 32, 0, s>>>(f, P, fresh);
+        k_force_sms<false><<<num_sms * shape.force_sms, kWarpsPerBlock * 32, 0, s>>>(f, P);
+    }
 }
 
 void launch_integrate(const Frame &f, const DevParams &P, cudaStream_t s) {

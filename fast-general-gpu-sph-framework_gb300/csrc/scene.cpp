@@ -234,6 +234,10 @@ DevParams make_dev_params(const gsph_params &p) {
     d.gy_acc = p.gravity[1];
     d.gz_acc = p.gravity[2];
     d.bmin = p.bound_min[0];
+    d.visc_artificial = 0;
+    d.art_coef = 0.f;
+    d.art_eps = 0.01f * p.kernel_2;
+    d.spiky = p.spiky_value;
     d.sparse_total = 96;   // gpu_model.cu:172-180
     d.sparse_self = 15;
     d.mid_total = 60;

@@ -13,6 +13,7 @@
 // Unlike the reference, a frame needs no host synchronisation (the TRA/SMS
 // counts stay on the device), so whole frames can be captured as CUDA graphs.
 #include <algorithm>
+#include <cmath>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -1655,6 +1656,26 @@ gsph_status gsph_set_tuning(gsph_handle h, const gsph_tuning *t) {
     }
     GSPH_CUDA(cudaStreamSynchronize(h->sys.stream));
     return h->sys.set_tuning(*t);
+}
+
+gsph_status gsph_set_viscosity_model(gsph_handle h, int model, float alpha, float c0) {
+    gsph_status st = check_handle(h);
+    if (st) return st;
+    if (model != GSPH_VISCOSITY_LAPLACIAN && model != GSPH_VISCOSITY_ARTIFICIAL) {
+        set_error("gsph_set_viscosity_model: unknown model %d", model);
+        return GSPH_ERR_INVALID_ARG;
+    }
+    if (model == GSPH_VISCOSITY_ARTIFICIAL &&
+        !(alpha > 0.f && c0 > 0.f && std::isfinite(alpha * c0))) {
+        set_error("gsph_set_viscosity_model: alpha and c0 must be positive and finite");
+        return GSPH_ERR_INVALID_ARG;
+    }
+    System &s = h->sys;
+    GSPH_CUDA(cudaStreamSynchronize(s.stream));
+    s.dp.visc_artificial = model == GSPH_VISCOSITY_ARTIFICIAL;
+    s.dp.art_coef = model == GSPH_VISCOSITY_ARTIFICIAL ? alpha * c0 : 0.f;
+    s.drop_graphs();   // the captured launches carry the old parameters
+    return GSPH_OK;
 }
 
 // Built-in candidates: four split-threshold sets (the reference's, all TRA,

@@ -368,6 +368,27 @@ gsph_status gsph_set_render_transform(gsph_handle h, const float ratio[3],
 gsph_status gsph_tuning_default(gsph_tuning *out);
 gsph_status gsph_get_tuning(gsph_handle h, gsph_tuning *out);
 gsph_status gsph_set_tuning(gsph_handle h, const gsph_tuning *t);
+
+/* Viscosity model of the force pass (every scene of a handle).
+ * GSPH_VISCOSITY_LAPLACIAN (the default) is the reference's: mu * visco_value
+ * * sum_j V_j (v_j - v_i)(h - r) with V_j = 1/rho_j (force_kernels.cu:378-435,
+ * 525-561), mu = gsph_params.viscosity.
+ * GSPH_VISCOSITY_ARTIFICIAL is Monaghan's artificial viscosity (Monaghan
+ * 1992) in place of it: for a pair approaching each other (v_ij . r_ij < 0,
+ * v_ij = v_i - v_j, r_ij = x_i - x_j, velocities = evaluated velocities),
+ *   mu_ij = h v_ij . r_ij / (r^2 + 0.01 h^2),
+ *   Pi_ij = -alpha c0 mu_ij / ((rho_i + rho_j) / 2),
+ * and the particle's force (the quantity the integrator divides by rho_i)
+ * gains -m rho_i sum_j Pi_ij grad W(r_ij), with the spiky gradient the
+ * pressure term uses. alpha > 0 and c0 > 0 (the speed of sound) are given.
+ * The reference has no such term (it is an option of this library, checked
+ * against the FP64 oracle). The model is a handle setting: it is not stored
+ * in snapshots, and scene servers use the default. */
+typedef enum {
+    GSPH_VISCOSITY_LAPLACIAN = 0,
+    GSPH_VISCOSITY_ARTIFICIAL = 1
+} gsph_viscosity_model;
+gsph_status gsph_set_viscosity_model(gsph_handle h, int model, float alpha, float c0);
 /* Times n_candidates tunings (NULL: a built-in grid of split thresholds and
  * CTAs per SM) on the handle's current state, frames_per_trial frames each
  * after one warm-up frame, restoring the state after every trial, and

@@ -52,6 +52,8 @@ def _load():
             "oracle_tasks": ([vp, vp, vp, vp, vp, C.c_long], C.c_long),
             "oracle_density": ([vp, vp, vp, C.c_long, vp, vp, vp], C.c_int),
             "oracle_force": ([vp, vp, vp, vp, C.c_long, vp, vp, vp], C.c_int),
+            "oracle_force_model": ([vp, vp, vp, vp, C.c_long, vp, C.c_int, C.c_double,
+                                    C.c_double, vp, vp], C.c_int),
             "oracle_integrate": ([vp, vp, vp, vp, C.c_long, vp], None),
             "oracle_step": ([vp, vp, vp, C.c_long, vp], C.c_int),
             "oracle_num_threads": ([], C.c_int),
@@ -203,17 +205,23 @@ def density(pos4_sorted, key_sorted, cell_start, params):
     return rho, pr
 
 
-def force(pos4_sorted, ev4_sorted, key_sorted, cell_start, params, with_mag=False):
+def force(pos4_sorted, ev4_sorted, key_sorted, cell_start, params, with_mag=False,
+          artificial=None):
     """FP64 force (n, 3); with_mag also returns the per-particle sum of pair
-    term magnitudes (the conditioning scale of the summation)."""
+    term magnitudes (the conditioning scale of the summation). artificial =
+    (alpha, c0) replaces the reference's Laplacian viscosity with Monaghan's
+    artificial viscosity."""
     p = np.ascontiguousarray(pos4_sorted, np.float32)
     e = np.ascontiguousarray(ev4_sorted, np.float32)
     n = len(p)
     acc = np.empty((n, 3), np.float64)
     mag = np.empty(n, np.float64)
-    if _load().oracle_force(_p(p), _p(e), _p(np.ascontiguousarray(key_sorted, np.uint32)),
-                            _p(np.ascontiguousarray(cell_start, np.int32)), n,
-                            _ref(params), _p(acc), _p(mag)) != 0:
+    model, alpha, c0 = (0, 0.0, 0.0) if artificial is None else (1, *artificial)
+    if _load().oracle_force_model(_p(p), _p(e),
+                                  _p(np.ascontiguousarray(key_sorted, np.uint32)),
+                                  _p(np.ascontiguousarray(cell_start, np.int32)), n,
+                                  _ref(params), model, float(alpha), float(c0),
+                                  _p(acc), _p(mag)) != 0:
         raise MemoryError("oracle_force allocation failed")
     return (acc, mag) if with_mag else acc
 

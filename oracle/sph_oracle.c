@@ -21,6 +21,9 @@
  *                        297-565 (FP64, full 27-cell search)
  *   oracle_force         src/solver/force_kernels.cu:378-435, 525-561,
  *                        725-1054 (FP64, full 27-cell search)
+ *   oracle_force_model   the same with Monaghan's artificial viscosity
+ *                        (Monaghan 1992) as an alternative to the reference's
+ *                        Laplacian term; the reference has no such option
  *   oracle_integrate     src/solver/integration_kernels.cu:235-336 (FP64)
  *   oracle_step          src/simulation/sph_hybrid_system.cpp:253-339 (FP64)
  *
@@ -380,11 +383,18 @@ static void density_d(const double *pos4, const uint32_t *key_sorted,
 }
 
 /* FP64 force core on double state (pos w = 1/rho, ev w = pressure). */
+/* model: 0 = the reference's Laplacian viscosity (force_kernels.cu:378-435);
+ * 1 = Monaghan's artificial viscosity (Monaghan 1992) in its place, with
+ * art_coef = alpha * c0: for v_ij . r_ij < 0, mu = h v_ij . r_ij /
+ * (r^2 + 0.01 h^2), Pi = -alpha c0 mu / ((rho_i + rho_j) / 2), force
+ * -m rho_i sum_j Pi grad W_spiky(r_ij). */
 static void force_d(const double *pos4, const double *ev4,
                     const uint32_t *key_sorted, const int32_t *cell_start,
-                    long n, const gsph_params *p, double *acc3, double *mag) {
+                    long n, const gsph_params *p, int model, double art_coef,
+                    double *acc3, double *mag) {
     const int gx = p->grid_size[0], gy = p->grid_size[1], gz = p->grid_size[2];
     const double h = (double)p->kernel, h2 = h * h;
+    const double art_eps = (double)(0.01f * p->kernel_2);
 #pragma omp parallel for schedule(dynamic, 1024)
     for (long i = 0; i < n; ++i) {
         int cx, cy, cz;
@@ -415,9 +425,25 @@ static void force_d(const double *pos4, const double *ev4,
                         P[2] -= rz * pw;
                         Pm += fabs(pw) * d;
                         const double wk = V * k;
-                        const double ux = (ev4[4 * j] - vxi) * wk;
-                        const double uy = (ev4[4 * j + 1] - vyi) * wk;
-                        const double uz = (ev4[4 * j + 2] - vzi) * wk;
+                        double ux, uy, uz;
+                        if (model == 1) {
+                            const double vr = (vxi - ev4[4 * j]) * rx +
+                                              (vyi - ev4[4 * j + 1]) * ry +
+                                              (vzi - ev4[4 * j + 2]) * rz;
+                            double w = 0.0;
+                            if (vr < 0.0) {
+                                const double mu = h * vr / (d2 + art_eps);
+                                const double rho_mean = 0.5 * (1.0 / inv_rho_i + 1.0 / V);
+                                w = -art_coef * mu / rho_mean * k * k / d;
+                            }
+                            ux = rx * w;
+                            uy = ry * w;
+                            uz = rz * w;
+                        } else {
+                            ux = (ev4[4 * j] - vxi) * wk;
+                            uy = (ev4[4 * j + 1] - vyi) * wk;
+                            uz = (ev4[4 * j + 2] - vzi) * wk;
+                        }
                         Vs[0] += ux;
                         Vs[1] += uy;
                         Vs[2] += uz;
@@ -430,11 +456,11 @@ static void force_d(const double *pos4, const double *ev4,
                         L += V * hr * (d2 - 0.75 * hr);
                     }
                 }
+        const double vcoef = model == 1 ? -(double)p->spiky_value / inv_rho_i
+                                        : (double)p->viscosity_visco_value;
         double F[3];
         for (int a = 0; a < 3; ++a)
-            F[a] = (P[a] * (double)p->half_spiky_value +
-                    Vs[a] * (double)p->viscosity_visco_value) *
-                   (double)p->mass;
+            F[a] = (P[a] * (double)p->half_spiky_value + Vs[a] * vcoef) * (double)p->mass;
         for (int a = 0; a < 3; ++a) G[a] *= (double)p->grad_color_scale;
         L *= (double)p->lplc_color_scale * inv_rho_i;
         const double nrm = sqrt(G[0] * G[0] + G[1] * G[1] + G[2] * G[2]);
@@ -445,8 +471,7 @@ static void force_d(const double *pos4, const double *ev4,
             acc3[3 * i + a] = F[a] + sf;
         }
         if (mag)
-            mag[i] = (Pm * fabs((double)p->half_spiky_value) +
-                      Vm * fabs((double)p->viscosity_visco_value)) *
+            mag[i] = (Pm * fabs((double)p->half_spiky_value) + Vm * fabs(vcoef)) *
                      (double)p->mass;
     }
 }
@@ -489,7 +514,27 @@ ORACLE_EXPORT int oracle_force(const float *pos4, const float *ev4,
         free(ed);
         return -2;
     }
-    force_d(pd, ed, key_sorted, cell_start, n, p, acc3, mag);
+    force_d(pd, ed, key_sorted, cell_start, n, p, 0, 0.0, acc3, mag);
+    free(pd);
+    free(ed);
+    return 0;
+}
+
+/* oracle_force with a choice of viscosity model (0: the reference's
+ * Laplacian; 1: Monaghan's artificial viscosity with alpha and c0). */
+ORACLE_EXPORT int oracle_force_model(const float *pos4, const float *ev4,
+                                     const uint32_t *key_sorted,
+                                     const int32_t *cell_start, long n,
+                                     const gsph_params *p, int model, double alpha,
+                                     double c0, double *acc3, double *mag) {
+    double *pd = widen(pos4, 4 * n), *ed = widen(ev4, 4 * n);
+    if (!pd || !ed) {
+        free(pd);
+        free(ed);
+        return -2;
+    }
+    force_d(pd, ed, key_sorted, cell_start, n, p, model,
+            (double)((float)alpha * (float)c0), acc3, mag);
     free(pd);
     free(ed);
     return 0;
@@ -587,7 +632,7 @@ ORACLE_EXPORT int oracle_step(double *pos4, double *vel4, double *ev4, long n,
         pos4[4 * i + 3] = 1.0 / rho[i];
         ev4[4 * i + 3] = rho[n + i];
     }
-    force_d(pos4, ev4, ks, cs, n, p, acc, NULL);
+    force_d(pos4, ev4, ks, cs, n, p, 0, 0.0, acc, NULL);
     oracle_integrate(pos4, vel4, ev4, acc, n, p);
     free(pf); free(ks); free(perm); free(cs); free(tmp); free(rho); free(acc);
     return bad;

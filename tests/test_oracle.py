@@ -220,3 +220,70 @@ def test_step_is_deterministic_and_conserves_count(gsph, oracle):
     assert len(a[0]) == len(pos)
     assert np.all(np.isfinite(a[0]))
     assert oracle.num_threads() >= 1
+
+
+def _force_inputs(oracle, p, pos, seed=1, v_scale=0.1):
+    ks, perm, cs, _ = oracle.sort(pos, p)
+    sp = pos[perm].copy()
+    rho, pr = oracle.density(sp, ks, cs, p)
+    sp[:, 3] = (1.0 / rho).astype(np.float32)
+    rng = np.random.default_rng(seed)
+    ev = np.zeros_like(sp)
+    ev[:, :3] = rng.normal(0, v_scale, (len(sp), 3))
+    ev[:, 3] = pr.astype(np.float32)
+    return sp, ev, ks, cs
+
+
+def brute_viscosity(sp, ev, p, alpha=None, c0=None):
+    """Viscosity part of the force, all pairs in numpy FP64: the reference's
+    Laplacian form m mu visco sum V_j (v_j - v_i)(h - r), or Monaghan's
+    artificial viscosity -m rho_i sum Pi_ij grad W_spiky (Monaghan 1992)."""
+    x = sp[:, :3].astype(np.float64)
+    v = ev[:, :3].astype(np.float64)
+    V = sp[:, 3].astype(np.float64)
+    r = x[:, None, :] - x[None, :, :]
+    d2 = (r ** 2).sum(-1)
+    h = float(p.kernel)
+    inside = (d2 <= h * h) & (d2 >= 1e-12)
+    d = np.sqrt(np.where(inside, d2, 1.0))
+    k = np.where(inside, h - d, 0.0)
+    m = float(p.mass)
+    if alpha is None:
+        w = V[None, :] * k
+        return m * float(p.viscosity_visco_value) * (w[:, :, None] * (v[None, :, :] - v[:, None, :])).sum(1)
+    vr = ((v[:, None, :] - v[None, :, :]) * r).sum(-1)
+    mu = h * vr / (d2 + float(np.float32(0.01) * np.float32(p.kernel_2)))
+    rho_mean = 0.5 * (1.0 / V[:, None] + 1.0 / V[None, :])
+    coef = float(np.float32(alpha) * np.float32(c0))
+    pij = np.where(inside & (vr < 0), -coef * mu / rho_mean, 0.0)
+    grad = float(p.spiky_value) * (k * k / d)[:, :, None] * r       # spiky gradient
+    return -m / V[:, None] * (pij[:, :, None] * grad).sum(1)
+
+
+def test_artificial_viscosity_matches_brute_force(gsph, oracle):
+    """The oracle's two viscosity models differ exactly by the difference of
+    the two brute-force viscosity terms (everything else is shared)."""
+    s, p, pos = small_scene(gsph, n_side=9)
+    sp, ev, ks, cs = _force_inputs(oracle, p, pos, v_scale=0.3)
+    lap = oracle.force(sp, ev, ks, cs, p)
+    art = oracle.force(sp, ev, ks, cs, p, artificial=(0.02, 20.0))
+    expect = brute_viscosity(sp, ev, p, 0.02, 20.0) - brute_viscosity(sp, ev, p)
+    scale = np.abs(expect).max()
+    assert scale > 0
+    np.testing.assert_allclose(art - lap, expect, rtol=0, atol=1e-9 * scale)
+    # approaching pairs only: with all particles receding from the centre the
+    # artificial term vanishes
+    c = sp[:, :3].astype(np.float64).mean(0)
+    ev2 = ev.copy()
+    ev2[:, :3] = (sp[:, :3] - c).astype(np.float32)
+    assert np.abs(brute_viscosity(sp, ev2, p, 0.02, 20.0)).max() == 0.0
+
+
+def test_artificial_viscosity_momentum_balance(gsph, oracle):
+    s, p, pos = small_scene(gsph, n_side=10)
+    p.surface_coe = 0.0
+    sp, ev, ks, cs = _force_inputs(oracle, p, pos, v_scale=0.5)
+    acc = oracle.force(sp, ev, ks, cs, p, artificial=(0.5, 20.0))
+    net = (acc * sp[:, 3:4].astype(np.float64)).sum(0)
+    scale = np.abs(acc * sp[:, 3:4]).sum(0)
+    assert np.all(np.abs(net) <= 1e-9 * scale + 1e-12)
