@@ -506,13 +506,18 @@ def served_record(g, W, S, args, R, rank, local, duration):
     trace = W.served_requests(duration, seed=1 + rank)
     budget = int(args.budget_gb * 1e9)
     cap = (args.cap_particles, (1 << 26) - 1, 4096)
+    # batches the server may open: as many as the budget holds at their
+    # capacity (each batch's key space holds fewer than 2^26 cells)
+    batch_bytes = S.scene_bytes(cap[0], cap[1])
+    max_batches = args.max_batches or max(1, budget // batch_bytes)
     native = args.server == "native"
     if native:
-        srv = g.NativeSceneServer(budget, cap, chunk=args.chunk, device=local)
+        srv = g.NativeSceneServer(budget, cap, chunk=args.chunk, device=local,
+                                  max_batches=max_batches)
         arrivals, finished = {}, {}
     else:
         srv = S.SceneServer(g, budget_bytes=budget, capacity=cap, chunk=args.chunk,
-                            device=local, keep_results=False)
+                            device=local, keep_results=False, max_batches=max_batches)
     # warm the library (context, modules) on a small scene outside the timed run
     p0, pos0 = W.build(g, {"nx": 16, "ny": 16, "nz": 16, "seed": 3})
     with g.HybridSystem(params=p0, positions=pos0, device=local) as h:
@@ -549,6 +554,7 @@ def served_record(g, W, S, args, R, rank, local, duration):
     busy = 0.0
     peak_resident = 0
     peak_particles = 0
+    peak_batches = 0
     if native:
         while True:
             tb = time.perf_counter()
@@ -559,6 +565,7 @@ def served_record(g, W, S, args, R, rank, local, duration):
             st = srv.stats()
             peak_resident = max(peak_resident, st["resident"])
             peak_particles = max(peak_particles, st["resident_particles"])
+            peak_batches = max(peak_batches, st["batches"])
             if k:
                 busy += now - tb
             elif done_submitting.is_set() and st["queued"] == 0 and st["resident"] == 0:
@@ -579,6 +586,7 @@ def served_record(g, W, S, args, R, rank, local, duration):
             if srv.resident:
                 peak_resident = max(peak_resident, len(srv.resident))
                 peak_particles = max(peak_particles, sum(r.n for r in srv.resident))
+                peak_batches = max(peak_batches, sum(1 for sh in srv.shards if sh.resident))
                 srv.step_chunk()
                 busy += time.perf_counter() - tb
             else:
@@ -610,6 +618,7 @@ def served_record(g, W, S, args, R, rank, local, duration):
         "host_s": host_s, "rejected": rejected,
         "budget_gb": args.budget_gb, "capacity_particles": cap[0],
         "capacity_cells": cap[1], "chunk_frames": args.chunk,
+        "max_batches": max_batches, "peak_batches": peak_batches,
         "server": "native gsph_server_*" if native else "Python SceneServer",
         "peak_resident_scenes": peak_resident, "peak_resident_particles": peak_particles,
         "per_scene_fifo_loop": loop,
@@ -638,11 +647,12 @@ def run_served(args, ws, rank, local):
                 "lattices built on arrival",
         "config": {"workload": "served: " + rec["workload"],
                    **{k: rec[k] for k in ("budget_gb", "capacity_particles",
-                                          "capacity_cells", "chunk_frames", "server")}},
+                                          "capacity_cells", "chunk_frames", "server",
+                                          "max_batches")}},
         **{k: rec[k] for k in ("latency", "requests", "offered_particle_steps",
                                "makespan_s", "server_busy_s", "host_s", "rejected",
                                "peak_resident_scenes", "peak_resident_particles",
-                               "per_scene_fifo_loop", "speedup_vs_loop", "p50_vs_loop",
+                               "peak_batches", "per_scene_fifo_loop", "speedup_vs_loop", "p50_vs_loop",
                                "p99_vs_loop", "clocks", "gpu_launches")},
     }
     if rank == 0:
@@ -671,6 +681,9 @@ def main():
     ap.add_argument("--cap-particles", type=int, default=40_000_000,
                     help="served: particle capacity of the resident batch")
     ap.add_argument("--chunk", type=int, default=10, help="served: frames between admissions")
+    ap.add_argument("--max-batches", type=int, default=0,
+                    help="served: batches the server may open (0: as many as the budget "
+                         "holds at their capacity)")
     ap.add_argument("--server", default="native", choices=["native", "python"],
                     help="served: the C++ server (gsph_server_*) or the Python SceneServer")
     ap.add_argument("--no-batched", action="store_true",

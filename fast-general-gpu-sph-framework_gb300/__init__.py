@@ -159,14 +159,14 @@ class ServerConfig(C.Structure):
     """gsph_server_config."""
     _fields_ = [("budget_bytes", C.c_uint64), ("particle_capacity", C.c_uint64),
                 ("cell_capacity", C.c_uint64), ("scene_capacity", C.c_uint32),
-                ("chunk_frames", C.c_int32), ("device", C.c_int32), ("reserved_", C.c_int32)]
+                ("chunk_frames", C.c_int32), ("device", C.c_int32), ("max_batches", C.c_int32)]
 
 
 class ServerStats(C.Structure):
     """gsph_server_stats."""
     _fields_ = [(n, C.c_uint64) for n in (
         "submitted", "finished", "rejected", "frames", "chunks", "particle_steps",
-        "queued", "resident", "resident_particles", "resident_bytes")]
+        "queued", "resident", "resident_particles", "resident_bytes", "batches")]
 
     def as_dict(self) -> dict:
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -587,10 +587,13 @@ class NativeSceneServer:
     from any thread, call step() from one thread, collect finished results
     with results()."""
 
-    def __init__(self, budget_bytes: int, capacity, chunk: int = 10, device: int = 0):
+    def __init__(self, budget_bytes: int, capacity, chunk: int = 10, device: int = 0,
+                 max_batches: int = 1):
+        """capacity = (particles, cells, scenes) of each batch; up to
+        max_batches batches are opened as admissions need them."""
         lib = load_library()
         cfg = ServerConfig(int(budget_bytes), int(capacity[0]), int(capacity[1]),
-                           int(capacity[2]), int(chunk), int(device), 0)
+                           int(capacity[2]), int(chunk), int(device), int(max_batches))
         h = C.c_void_p()
         _check(lib.gsph_server_create(C.byref(cfg), C.byref(h)))
         self._h = h

@@ -4,8 +4,10 @@
 // is the native counterpart of a request loop: requests (a scene's initial
 // state and a number of frames) wait in a FIFO queue and are admitted between
 // chunks of frames while the resident scenes' device state fits the memory
-// budget and the batch's capacity. All resident scenes are stepped together by
-// one batch handle (one launch per stage for all of them); a chunk stops at
+// budget; each goes to a batch with room for it (capacity: particles, cells,
+// scenes), and a new batch is opened while fewer than max_batches are. The
+// resident scenes of a batch are stepped together (one launch per stage for
+// all of them), the batches on their own streams at once; a chunk stops at
 // the earliest completion, so every request is stepped exactly its frames;
 // finished requests leave the batch (gsph_batch_repack, together with the
 // admissions of the next step) and their final state waits for
@@ -48,12 +50,20 @@ struct Request {
 
 }  // namespace
 
+// One batch handle and the requests resident in it (in batch order). A
+// batch's key space holds at most 2^26 cells, so the server opens further
+// batches (up to max_batches) rather than let the key space cap residency:
+// the memory budget is what bounds the resident scenes.
+struct Shard {
+    gsph_handle batch = nullptr;
+    std::vector<Request> resident;
+};
+
 struct gsph_server {
     gsph_server_config cfg{};
-    gsph_handle batch = nullptr;
-    std::mutex mu;                       // queue, finished, stats
+    std::vector<Shard> shards;
+    std::mutex mu;                       // queue, finished, stats, residents' counters
     std::deque<Request> queue;
-    std::vector<Request> resident;       // batch order
     std::deque<uint64_t> finished_order;
     std::unordered_map<uint64_t, Request> finished;
     gsph_server_stats stats{};
@@ -71,6 +81,10 @@ uint64_t cells_of(const gsph_params &p) {
     return uint64_t(p.grid_size[0]) * uint64_t(p.grid_size[1]) * uint64_t(p.grid_size[2]);
 }
 
+int max_batches(const gsph_server_config &cfg) {
+    return cfg.max_batches > 0 ? cfg.max_batches : 1;
+}
+
 }  // namespace
 
 extern "C" {
@@ -83,7 +97,7 @@ gsph_status gsph_server_create(const gsph_server_config *cfg, gsph_server_handle
     *out = nullptr;
     if (cfg->chunk_frames < 1 || cfg->particle_capacity == 0 || cfg->cell_capacity == 0 ||
         cfg->scene_capacity == 0 || cfg->particle_capacity > 0x7FFFFFFFull ||
-        cfg->cell_capacity >= 67108864ull) {
+        cfg->cell_capacity >= 67108864ull || cfg->max_batches < 0) {
         fail("gsph_server_create: chunk_frames >= 1 and capacities in range needed");
         return GSPH_ERR_INVALID_ARG;
     }
@@ -99,7 +113,8 @@ gsph_status gsph_server_create(const gsph_server_config *cfg, gsph_server_handle
 
 gsph_status gsph_server_destroy(gsph_server_handle s) {
     if (!s) return GSPH_OK;
-    if (s->batch) gsph_destroy(s->batch);
+    for (Shard &sh : s->shards)
+        if (sh.batch) gsph_destroy(sh.batch);
     delete s;
     return GSPH_OK;
 }
@@ -130,6 +145,48 @@ gsph_status gsph_server_submit(gsph_server_handle s, uint64_t id, const gsph_par
     return GSPH_OK;
 }
 
+namespace {
+
+// Per-shard totals of the scenes that stay and of the ones admitted now.
+struct ShardPlan {
+    std::vector<uint32_t> keep;
+    std::vector<Request> admitted;
+    uint64_t n = 0, c = 0;
+};
+
+// Creates or repacks shard `sh` for its plan.
+gsph_status apply_plan(const gsph_server_config &cfg, Shard &sh, ShardPlan &pl) {
+    std::vector<gsph_params> plist;
+    std::vector<uint32_t> counts;
+    std::vector<float> pos, vel;
+    bool any_vel = false;
+    for (const Request &r : pl.admitted) any_vel |= !r.vel.empty();
+    for (const Request &r : pl.admitted) {
+        plist.push_back(r.params);
+        counts.push_back(r.n);
+        pos.insert(pos.end(), r.pos.begin(), r.pos.end());
+        if (any_vel) {
+            if (r.vel.empty())
+                vel.insert(vel.end(), size_t(r.n) * 4, 0.f);
+            else
+                vel.insert(vel.end(), r.vel.begin(), r.vel.end());
+        }
+    }
+    if (!sh.batch)
+        return gsph_batch_create_ex(plist.data(), counts.data(), uint32_t(plist.size()),
+                                    pos.empty() ? nullptr : pos.data(),
+                                    any_vel ? vel.data() : nullptr, cfg.particle_capacity,
+                                    cfg.cell_capacity, cfg.scene_capacity, cfg.device,
+                                    &sh.batch);
+    return gsph_batch_repack(sh.batch, pl.keep.empty() ? nullptr : pl.keep.data(),
+                             uint32_t(pl.keep.size()), plist.empty() ? nullptr : plist.data(),
+                             counts.empty() ? nullptr : counts.data(), uint32_t(plist.size()),
+                             pos.empty() ? nullptr : pos.data(),
+                             any_vel ? vel.data() : nullptr);
+}
+
+}  // namespace
+
 gsph_status gsph_server_step(gsph_server_handle s, int *frames_stepped) {
     if (!s) {
         fail("gsph_server_step: null server");
@@ -137,30 +194,50 @@ gsph_status gsph_server_step(gsph_server_handle s, int *frames_stepped) {
     }
     if (frames_stepped) *frames_stepped = 0;
     const gsph_server_config &cfg = s->cfg;
-    // 1. retire finished scenes and admit queued requests that fit (FIFO)
-    std::vector<uint32_t> keep;
-    uint64_t n = 0, c = 0, bytes = 0;
-    for (size_t k = 0; k < s->resident.size(); ++k) {
-        const Request &r = s->resident[k];
-        if (r.remaining == 0) continue;
-        keep.push_back(uint32_t(k));
-        n += r.n;
-        c += r.cells;
-        bytes += r.bytes();
+    // 1. retire finished scenes and admit queued requests that fit (FIFO): a
+    //    request goes to the first batch with room for it, or to a new batch
+    //    while fewer than max_batches are open; the budget bounds the resident
+    //    bytes of all batches together
+    std::vector<ShardPlan> plan(s->shards.size());
+    uint64_t bytes = 0;
+    for (size_t b = 0; b < s->shards.size(); ++b) {
+        const std::vector<Request> &res = s->shards[b].resident;
+        for (size_t k = 0; k < res.size(); ++k) {
+            const Request &r = res[k];
+            if (r.remaining == 0) continue;
+            plan[b].keep.push_back(uint32_t(k));
+            plan[b].n += r.n;
+            plan[b].c += r.cells;
+            bytes += r.bytes();
+        }
     }
-    std::vector<Request> admitted;
+    size_t n_admitted = 0;
     {
         std::lock_guard<std::mutex> lock(s->mu);
         for (;;) {
             while (!s->queue.empty()) {
                 const Request &h = s->queue.front();
-                const uint64_t scenes = keep.size() + admitted.size() + 1;
-                if (!fits(cfg, n + h.n, c + h.cells, scenes, bytes + h.bytes())) break;
-                n += h.n;
-                c += h.cells;
+                if (bytes + h.bytes() > cfg.budget_bytes) break;
+                size_t b = 0;
+                for (; b < plan.size(); ++b) {
+                    const ShardPlan &pl = plan[b];
+                    const uint64_t scenes = pl.keep.size() + pl.admitted.size() + 1;
+                    if (fits(cfg, pl.n + h.n, pl.c + h.cells, scenes, 0)) break;
+                }
+                if (b == plan.size()) {
+                    // a new batch, if one may be opened and the head fits it
+                    if (int(plan.size()) >= max_batches(cfg) ||
+                        !fits(cfg, h.n, h.cells, 1, 0))
+                        break;
+                    plan.emplace_back();
+                }
+                ShardPlan &pl = plan[b];
+                pl.n += h.n;
+                pl.c += h.cells;
                 bytes += h.bytes();
-                admitted.push_back(std::move(s->queue.front()));
+                pl.admitted.push_back(std::move(s->queue.front()));
                 s->queue.pop_front();
+                ++n_admitted;
             }
             // a head that cannot fit even alone would block the queue forever
             if (!s->queue.empty()) {
@@ -174,95 +251,83 @@ gsph_status gsph_server_step(gsph_server_handle s, int *frames_stepped) {
             break;
         }
     }
-    const bool changed = !admitted.empty() || keep.size() != s->resident.size();
-    if (changed) {
-        std::vector<gsph_params> plist;
-        std::vector<uint32_t> counts;
-        std::vector<float> pos, vel;
-        bool any_vel = false;
-        for (const Request &r : admitted) any_vel |= !r.vel.empty();
-        for (const Request &r : admitted) {
-            plist.push_back(r.params);
-            counts.push_back(r.n);
-            pos.insert(pos.end(), r.pos.begin(), r.pos.end());
-            if (any_vel) {
-                if (r.vel.empty())
-                    vel.insert(vel.end(), size_t(r.n) * 4, 0.f);
-                else
-                    vel.insert(vel.end(), r.vel.begin(), r.vel.end());
-            }
-        }
-        gsph_status st;
-        if (!s->batch) {
-            if (admitted.empty()) return GSPH_OK;
-            st = gsph_batch_create_ex(plist.data(), counts.data(), uint32_t(plist.size()),
-                                      pos.empty() ? nullptr : pos.data(),
-                                      any_vel ? vel.data() : nullptr, cfg.particle_capacity,
-                                      cfg.cell_capacity, cfg.scene_capacity, cfg.device,
-                                      &s->batch);
-        } else {
-            st = gsph_batch_repack(s->batch, keep.empty() ? nullptr : keep.data(),
-                                   uint32_t(keep.size()),
-                                   plist.empty() ? nullptr : plist.data(),
-                                   counts.empty() ? nullptr : counts.data(),
-                                   uint32_t(plist.size()), pos.empty() ? nullptr : pos.data(),
-                                   any_vel ? vel.data() : nullptr);
-        }
+    if (plan.size() > s->shards.size()) s->shards.resize(plan.size());
+    for (size_t b = 0; b < plan.size(); ++b) {
+        Shard &sh = s->shards[b];
+        ShardPlan &pl = plan[b];
+        const bool changed = !pl.admitted.empty() || pl.keep.size() != sh.resident.size();
+        if (!changed) continue;
+        gsph_status st = (sh.batch || !pl.admitted.empty()) ? apply_plan(cfg, sh, pl)
+                                                             : GSPH_OK;
         if (st) {
-            // put the admitted requests back at the head of the queue
+            // this and the later batches' admissions go back to the head of
+            // the queue, in their order
+            std::vector<Request> back;
+            for (size_t q = b; q < plan.size(); ++q)
+                for (Request &r : plan[q].admitted) back.push_back(std::move(r));
             std::lock_guard<std::mutex> lock(s->mu);
-            for (auto it = admitted.rbegin(); it != admitted.rend(); ++it)
+            for (auto it = back.rbegin(); it != back.rend(); ++it)
                 s->queue.push_front(std::move(*it));
             return st;
         }
         std::lock_guard<std::mutex> lock(s->mu);
         std::vector<Request> next;
-        next.reserve(keep.size() + admitted.size());
-        for (uint32_t k : keep) next.push_back(std::move(s->resident[k]));
-        for (Request &r : admitted) {
+        next.reserve(pl.keep.size() + pl.admitted.size());
+        for (uint32_t k : pl.keep) next.push_back(std::move(sh.resident[k]));
+        for (Request &r : pl.admitted) {
             r.pos.clear();
             r.pos.shrink_to_fit();
             r.vel.clear();
             r.vel.shrink_to_fit();
             next.push_back(std::move(r));
         }
-        s->resident = std::move(next);
+        sh.resident = std::move(next);
     }
-    if (s->resident.empty()) return GSPH_OK;
-    // 2. step all resident scenes up to the earliest completion
+    (void)n_admitted;
+    // 2. step all resident scenes up to the earliest completion: every batch
+    //    is launched on its own stream first, then all are waited for
     uint32_t k = uint32_t(cfg.chunk_frames);
     uint64_t resident_n = 0;
-    for (const Request &r : s->resident) {
-        k = std::min(k, r.remaining);
-        resident_n += r.n;
-    }
-    gsph_status st = gsph_step(s->batch, int(k));
-    if (!st) st = gsph_sync(s->batch);
-    if (st) return st;
+    bool any = false;
+    for (const Shard &sh : s->shards)
+        for (const Request &r : sh.resident) {
+            k = std::min(k, r.remaining);
+            resident_n += r.n;
+            any = true;
+        }
+    if (!any) return GSPH_OK;
+    gsph_status st = GSPH_OK;
+    for (Shard &sh : s->shards)
+        if (!sh.resident.empty() && (st = gsph_step(sh.batch, int(k)))) return st;
+    for (Shard &sh : s->shards)
+        if (!sh.resident.empty() && (st = gsph_sync(sh.batch))) return st;
     // 3. read back the finished requests' final state
     {
         std::lock_guard<std::mutex> lock(s->mu);
-        for (Request &r : s->resident) r.remaining -= k;
+        for (Shard &sh : s->shards)
+            for (Request &r : sh.resident) r.remaining -= k;
     }
     std::vector<Request> done;
-    for (size_t i = 0; i < s->resident.size(); ++i) {
-        const Request &r = s->resident[i];
-        if (r.remaining) continue;
-        Request out;
-        out.id = r.id;
-        out.params = r.params;
-        out.n = r.n;
-        out.frames = r.frames;
-        out.pos.resize(size_t(r.n) * 4);
-        out.vel.resize(size_t(r.n) * 4);
-        if (r.n) {
-            if ((st = gsph_copy_out_scene(s->batch, uint32_t(i), GSPH_FIELD_POSITION,
-                                          out.pos.data(), out.pos.size() * 4)) ||
-                (st = gsph_copy_out_scene(s->batch, uint32_t(i), GSPH_FIELD_VELOCITY,
-                                          out.vel.data(), out.vel.size() * 4)))
-                return st;
+    for (Shard &sh : s->shards) {
+        for (size_t i = 0; i < sh.resident.size(); ++i) {
+            const Request &r = sh.resident[i];
+            if (r.remaining) continue;
+            Request out;
+            out.id = r.id;
+            out.params = r.params;
+            out.n = r.n;
+            out.frames = r.frames;
+            out.pos.resize(size_t(r.n) * 4);
+            out.vel.resize(size_t(r.n) * 4);
+            if (r.n) {
+                if ((st = gsph_copy_out_scene(sh.batch, uint32_t(i), GSPH_FIELD_POSITION,
+                                              out.pos.data(), out.pos.size() * 4)) ||
+                    (st = gsph_copy_out_scene(sh.batch, uint32_t(i), GSPH_FIELD_VELOCITY,
+                                              out.vel.data(), out.vel.size() * 4)))
+                    return st;
+            }
+            done.push_back(std::move(out));
         }
-        done.push_back(std::move(out));
     }
     std::lock_guard<std::mutex> lock(s->mu);
     for (Request &r : done) {
@@ -321,14 +386,19 @@ gsph_status gsph_server_get_stats(gsph_server_handle s, gsph_server_stats *out) 
     std::lock_guard<std::mutex> lock(s->mu);
     *out = s->stats;
     out->queued = s->queue.size();
-    out->resident = s->resident.size();
-    uint64_t n = 0, bytes = 0;
-    for (const Request &r : s->resident) {
-        n += r.n;
-        bytes += r.bytes();
+    uint64_t n = 0, bytes = 0, scenes = 0, batches = 0;
+    for (const Shard &sh : s->shards) {
+        scenes += sh.resident.size();
+        batches += sh.resident.empty() ? 0 : 1;
+        for (const Request &r : sh.resident) {
+            n += r.n;
+            bytes += r.bytes();
+        }
     }
+    out->resident = scenes;
     out->resident_particles = n;
     out->resident_bytes = bytes;
+    out->batches = batches;
     return GSPH_OK;
 }
 

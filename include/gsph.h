@@ -265,7 +265,8 @@ gsph_status gsph_batch_repack(gsph_handle h, const uint32_t *keep, uint32_t n_ke
  * steps one scene per process). Requests — a scene's parameters, initial
  * positions (and velocities) and a number of frames — wait in a FIFO queue;
  * gsph_server_step admits the queued requests that fit the memory budget and
- * the batch capacity, steps every resident scene together up to the earliest
+ * a batch's capacity (opening batches up to max_batches), steps every resident
+ * scene together up to the earliest
  * completion (at most chunk_frames frames), and keeps the finished requests'
  * final state for gsph_server_take. Each request is stepped exactly its
  * frames, and its result is bit-identical to the scene stepped alone. A
@@ -276,17 +277,22 @@ gsph_status gsph_batch_repack(gsph_handle h, const uint32_t *keep, uint32_t n_ke
 typedef struct gsph_server *gsph_server_handle;
 typedef struct {
     uint64_t budget_bytes;         /* device bytes the resident scenes may use */
-    uint64_t particle_capacity;    /* batch capacity: particles, cells, scenes */
-    uint64_t cell_capacity;
+    uint64_t particle_capacity;    /* capacity of each batch: particles, cells, */
+    uint64_t cell_capacity;        /* scenes (a batch holds < 2^26 cells)       */
     uint32_t scene_capacity;
     int32_t chunk_frames;          /* most frames between admissions (>= 1) */
     int32_t device;
-    int32_t reserved_;
+    int32_t max_batches;           /* batches the server may open (0 or 1: one).
+                                    * Each opened batch allocates its capacity;
+                                    * the batches step concurrently on their
+                                    * own streams, and the budget bounds the
+                                    * resident bytes of all of them together. */
 } gsph_server_config;
 typedef struct {
     uint64_t submitted, finished, rejected;
     uint64_t frames, chunks, particle_steps;
     uint64_t queued, resident, resident_particles, resident_bytes;
+    uint64_t batches;              /* batches holding resident scenes */
 } gsph_server_stats;
 gsph_status gsph_server_create(const gsph_server_config *cfg, gsph_server_handle *out);
 gsph_status gsph_server_destroy(gsph_server_handle s);

@@ -87,3 +87,30 @@ def test_native_server_threads_and_rejection(gsph, cuda_device):
     assert sorted(got) == [reqs[0][0], reqs[1][0], reqs[2][0]]
     for rid, (pos, vel) in got.items():
         assert np.array_equal(pos.view(np.uint32), alone[rid][0].view(np.uint32)), rid
+
+
+def test_native_server_spreads_over_batches(gsph, cuda_device):
+    """Each batch's cell capacity holds about two of these scenes; with up to
+    three batches the server keeps more scenes resident (stepped together on
+    three streams) and every result still equals the scene stepped alone."""
+    reqs = _requests(gsph)
+    alone = _alone(gsph, reqs)
+    cells = max(int(r[1].numc) for r in reqs)
+    got = {}
+    peak_batches = 0
+    with gsph.NativeSceneServer(1 << 34, (200000, 2 * cells + 1, 8), chunk=4,
+                                max_batches=3) as srv:
+        for r in reqs:
+            srv.submit(r[0], r[1], r[2], r[3])
+        for _ in range(400):
+            srv.step()
+            got.update(srv.results())
+            st = srv.stats()
+            peak_batches = max(peak_batches, st["batches"])
+            if st["queued"] == 0 and st["resident"] == 0:
+                break
+    assert peak_batches >= 2
+    assert sorted(got) == [r[0] for r in reqs]
+    for rid, (pos, vel) in got.items():
+        assert np.array_equal(pos.view(np.uint32), alone[rid][0].view(np.uint32)), rid
+        assert np.array_equal(vel.view(np.uint32), alone[rid][1].view(np.uint32)), rid

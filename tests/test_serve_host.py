@@ -131,3 +131,36 @@ def test_latency_stats():
     assert st["p50_ms"] == pytest.approx(50.5)
     assert st["p99_ms"] == pytest.approx(99.01)
     assert S.latency_stats([])["p99_ms"] is None
+
+
+def test_batches_open_until_the_budget_binds():
+    """With several batches allowed, a full batch (its cell capacity, the
+    key space of one batch) does not stop admission: further batches open
+    and the memory budget is what bounds the resident scenes, exactly."""
+    S = _serve()
+    FakeBatch.log = []
+    per = S.scene_bytes(1000, 2000)
+    # each batch holds 3 scenes' cells; the budget holds exactly 7 scenes
+    srv = S.SceneServer(FakeG, budget_bytes=7 * per, capacity=(10**9, 6000, 64),
+                        chunk=100, clock=lambda: 0.0, max_batches=10)
+    for i in range(10):
+        srv.submit(_req(S, i, 1000, 10 + i))
+    assert srv.admit() == 7
+    assert [len(sh.resident) for sh in srv.shards] == [3, 3, 1]
+    assert sum(S.scene_bytes(r.n, r.cells) for r in srv.resident) == 7 * per
+    assert [r.rid for r in srv.resident] == list(range(7))
+    srv.step_chunk()                      # request 0 retires after 10 frames
+    assert srv.admit() == 1               # FIFO: request 7 takes its place
+    assert sorted(r.rid for r in srv.resident) == list(range(1, 8))
+    while srv.queue or srv.resident:
+        srv.admit()
+        srv.step_chunk()
+    assert sorted(r.rid for r in srv.done) == list(range(10))
+    for r in srv.done:
+        assert r.result["pos"] == r.steps
+    # one batch only: the cell capacity binds first
+    srv = S.SceneServer(FakeG, budget_bytes=7 * per, capacity=(10**9, 6000, 64),
+                        chunk=100, clock=lambda: 0.0, max_batches=1)
+    for i in range(10):
+        srv.submit(_req(S, i, 1000, 10 + i))
+    assert srv.admit() == 3
