@@ -145,14 +145,15 @@ class Info(C.Structure):
 
 
 class Tuning(C.Structure):
-    """gsph_tuning: split thresholds and CTAs per SM of the density/force
-    kernels (defaults: the reference's 96 / 15 / 60 and 6 / 6 / 4 / 4)."""
+    """gsph_tuning: split thresholds, CTAs per SM of the density/force kernels
+    and their warps per block (defaults: the reference's 96 / 15 / 60,
+    6 / 4 / 4 / 4 CTAs of 8 warps)."""
     _fields_ = [(n, C.c_int32) for n in (
         "sparse_total", "sparse_self", "mid_total", "ctas_density_tra",
-        "ctas_density_sms", "ctas_force_tra", "ctas_force_sms", "reserved_")]
+        "ctas_density_sms", "ctas_force_tra", "ctas_force_sms", "warps_per_block")]
 
     def as_dict(self) -> dict:
-        return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved_"}
+        return {n: getattr(self, n) for n, _ in self._fields_}
 
 
 class ServerConfig(C.Structure):

@@ -252,8 +252,9 @@ void launch_split(const Frame &f, const DevParams &P, int max_occ, int num_sms,
 // Launch shapes of the density and force passes: CTAs per SM of each kernel.
 struct LaunchShape {
     int density_tra, density_sms, force_tra, force_sms;
+    int warps;   // warps per block: 8, or 4 (then up to twice the CTAs per SM)
 };
-constexpr LaunchShape kMaxShape = {6, 4, 4, 4};   // the kernels' launch bounds
+constexpr LaunchShape kMaxShape = {6, 4, 4, 4, 8};   // the kernels' launch bounds
 
 // Shared-memory carveouts of the density and force kernels (once per
 // device, before their first launch).

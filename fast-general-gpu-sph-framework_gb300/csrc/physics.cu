@@ -300,6 +300,9 @@ __device__ __forceinline__ void write_force(const Frame &f, const DevParams &P,
     }
 }
 
+// Warps per block of the density and force kernels: 8 by default; each
+// kernel is also built for 4 (gsph_tuning.warps_per_block), with twice the
+// CTAs per SM for the same occupancy.
 constexpr int kWarpsPerBlock = 8;
 // SMS candidates staged per batch (two per lane).
 constexpr int kSmsBatch = 64;
@@ -318,7 +321,8 @@ __device__ __forceinline__ int next_unit(int *counter) {
 // One particle per lane, 32 consecutive TRA particles per work unit
 // (density_kernels.cu:318-366). Which candidates of each row interact is also
 // recorded as a bit mask for the force pass.
-__global__ void __launch_bounds__(kWarpsPerBlock * 32, 6)
+template <int W>
+__global__ void __launch_bounds__(W * 32, 6 * kWarpsPerBlock / W)
 k_density_tra(Frame f, DevParams P) {
     const int lane = threadIdx.x & 31;
     const int middle = f.ctr->middle;
@@ -482,11 +486,12 @@ __device__ __forceinline__ void task_z_range(const Frame &f, int self, bool acti
 // (x, x, y, y) float4 and a (z, z) float2; every lane evaluates them two at a
 // time with packed FP32x2 arithmetic (distances and h^2 - r^2 round exactly
 // as the scalar form).
-__global__ void __launch_bounds__(kWarpsPerBlock * 32, 4)
+template <int W>
+__global__ void __launch_bounds__(W * 32, 4 * kWarpsPerBlock / W)
 k_density_sms(Frame f, DevParams P) {
     // candidate pair k (slots 2k, 2k+1): (x, x, y, y) and (z, z)
-    __shared__ __align__(16) float4 sms_xy[kWarpsPerBlock][kDenBatch / 2];
-    __shared__ __align__(16) float2 sms_zz[kWarpsPerBlock][kDenBatch / 2];
+    __shared__ __align__(16) float4 sms_xy[W][kDenBatch / 2];
+    __shared__ __align__(16) float2 sms_zz[W][kDenBatch / 2];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int task_count = f.ctr->task_count;
@@ -555,11 +560,11 @@ k_density_sms(Frame f, DevParams P) {
 // mask) pairs in shared memory and walks all its neighbours in one loop, so
 // lanes stay converged across rows. Without masks (or with a row longer than
 // 32 candidates) the lane scans its candidates as the reference does.
-template <bool kArt>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32, 4)
+template <bool kArt, int W>
+__global__ void __launch_bounds__(W * 32, 4 * kWarpsPerBlock / W)
 k_force_tra(Frame f, DevParams P, bool fresh) {
-    __shared__ uint32_t row_mask[9][kWarpsPerBlock * 32];
-    __shared__ int row_start[9][kWarpsPerBlock * 32];
+    __shared__ uint32_t row_mask[9][W * 32];
+    __shared__ int row_start[9][W * 32];
     const int lane = threadIdx.x & 31;
     const int middle = f.ctr->middle;
     const int units = (middle + 31) >> 5;
@@ -657,12 +662,12 @@ k_force_tra(Frame f, DevParams P, bool fresh) {
 // skipped when no lane of the warp interacts with either candidate. Each
 // term rounds as the reference's scalar expression; the two halves of every
 // accumulator are summed at the end.
-template <bool kArt>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32, 4)
+template <bool kArt, int W>
+__global__ void __launch_bounds__(W * 32, 4 * kWarpsPerBlock / W)
 k_force_sms(Frame f, DevParams P) {
     // candidate pair k (slots 2k, 2k+1) as four float4s: (x, x, y, y),
     // (z, z, 1/rho, 1/rho), (vx, vx, vy, vy), (vz, vz, p, p)
-    __shared__ __align__(16) float4 sm[4][kWarpsPerBlock][kSmsBatch / 2];
+    __shared__ __align__(16) float4 sm[4][W][kSmsBatch / 2];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int task_count = f.ctr->task_count;
@@ -959,7 +964,7 @@ k_final_sum(const double *__restrict__ part, int nparts, double *__restrict__ ou
 // (static shared memory plus the 1 KB the SM reserves per CTA), so that the
 // rest of the SM's unified L1/shared storage stays L1 for candidate reads.
 template <class Kernel>
-cudaError_t set_carveout(Kernel kernel, int ctas, int smem_per_sm) {
+cudaError_t set_carveout(Kernel kernel, int ctas, int smem_per_sm, int threads) {
     cudaFuncAttributes a{};
     cudaError_t e = cudaFuncGetAttributes(&a, kernel);
     if (e != cudaSuccess) return e;
@@ -973,12 +978,43 @@ cudaError_t set_carveout(Kernel kernel, int ctas, int smem_per_sm) {
     // the hint is rounded to a supported split; keep the default if the
     // rounded one would hold fewer CTAs
     int fit = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kernel, kWarpsPerBlock * 32, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kernel, threads, 0);
     if (e != cudaSuccess) return e;
     if (fit < ctas)
         e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  int(cudaSharedmemCarveoutDefault));
     return e;
+}
+
+template <int W>
+cudaError_t configure_shape(int smem) {
+    const int k = kWarpsPerBlock / W;   // CTAs per SM scale with the block size
+    cudaError_t e;
+    if ((e = set_carveout(k_density_tra<W>, kMaxShape.density_tra * k, smem, W * 32)))
+        return e;
+    if ((e = set_carveout(k_density_sms<W>, kMaxShape.density_sms * k, smem, W * 32)))
+        return e;
+    if ((e = set_carveout(k_force_tra<false, W>, kMaxShape.force_tra * k, smem, W * 32)))
+        return e;
+    if ((e = set_carveout(k_force_tra<true, W>, kMaxShape.force_tra * k, smem, W * 32)))
+        return e;
+    if ((e = set_carveout(k_force_sms<false, W>, kMaxShape.force_sms * k, smem, W * 32)))
+        return e;
+    return set_carveout(k_force_sms<true, W>, kMaxShape.force_sms * k, smem, W * 32);
+}
+
+template <int W>
+void launch_density_w(const Frame &f, const DevParams &P, int num_sms,
+                      const LaunchShape &shape, cudaStream_t s) {
+    k_density_tra<W><<<num_sms * shape.density_tra, W * 32, 0, s>>>(f, P);
+    k_density_sms<W><<<num_sms * shape.density_sms, W * 32, 0, s>>>(f, P);
+}
+
+template <bool kArt, int W>
+void launch_force_w(const Frame &f, const DevParams &P, int num_sms, bool fresh,
+                    const LaunchShape &shape, cudaStream_t s) {
+    k_force_tra<kArt, W><<<num_sms * shape.force_tra, W * 32, 0, s>>>(f, P, fresh);
+    k_force_sms<kArt, W><<<num_sms * shape.force_sms, W * 32, 0, s>>>(f, P);
 }
 
 }  // namespace
@@ -988,30 +1024,33 @@ cudaError_t configure_physics_kernels(int device) {
     cudaError_t e = cudaDeviceGetAttribute(
         &smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device);
     if (e != cudaSuccess) return e;
-    if ((e = set_carveout(k_density_tra, kMaxShape.density_tra, smem))) return e;
-    if ((e = set_carveout(k_density_sms, kMaxShape.density_sms, smem))) return e;
-    if ((e = set_carveout(k_force_tra<false>, kMaxShape.force_tra, smem))) return e;
-    if ((e = set_carveout(k_force_tra<true>, kMaxShape.force_tra, smem))) return e;
-    if ((e = set_carveout(k_force_sms<false>, kMaxShape.force_sms, smem))) return e;
-    return set_carveout(k_force_sms<true>, kMaxShape.force_sms, smem);
+    if ((e = configure_shape<kWarpsPerBlock>(smem))) return e;
+    return configure_shape<kWarpsPerBlock / 2>(smem);
 }
 
 void launch_density(const Frame &f, const DevParams &P, int num_sms,
                     const LaunchShape &shape, cudaStream_t s) {
     if (f.n <= 0) return;
-    k_density_tra<<<num_sms * shape.density_tra, kWarpsPerBlock * 32, 0, s>>>(f, P);
-    k_density_sms<<<num_sms * shape.density_sms, kWarpsPerBlock * 32, 0, s>>>(f, P);
+    if (shape.warps == kWarpsPerBlock / 2)
+        launch_density_w<kWarpsPerBlock / 2>(f, P, num_sms, shape, s);
+    else
+        launch_density_w<kWarpsPerBlock>(f, P, num_sms, shape, s);
 }
 
 void launch_force(const Frame &f, const DevParams &P, int num_sms, bool fresh,
                   const LaunchShape &shape, cudaStream_t s) {
     if (f.n <= 0) return;
+    const bool half = shape.warps == kWarpsPerBlock / 2;
     if (P.visc_artificial) {
-        k_force_tra<true><<<num_sms * shape.force_tra, kWarpsPerBlock * 32, 0, s>>>(f, P, fresh);
-        k_force_sms<true><<<num_sms * shape.force_sms, kWarpsPerBlock * 32, 0, s>>>(f, P);
+        if (half)
+            launch_force_w<true, kWarpsPerBlock / 2>(f, P, num_sms, fresh, shape, s);
+        else
+            launch_force_w<true, kWarpsPerBlock>(f, P, num_sms, fresh, shape, s);
     } else {
-        k_force_tra<false><<<num_sms * shape.force_tra, kWarpsPerBlock * 32, 0, s>>>(f, P, fresh);
-        k_force_sms<false><<<num_sms * shape.force_sms, kWarpsPerBlock * 32, 0, s>>>(f, P);
+        if (half)
+            launch_force_w<false, kWarpsPerBlock / 2>(f, P, num_sms, fresh, shape, s);
+        else
+            launch_force_w<false, kWarpsPerBlock>(f, P, num_sms, fresh, shape, s);
     }
 }
 

@@ -715,25 +715,31 @@ struct System {
         t.ctas_density_sms = shape.density_sms;
         t.ctas_force_tra = shape.force_tra;
         t.ctas_force_sms = shape.force_sms;
+        t.warps_per_block = shape.warps;
         return t;
     }
 
     gsph_status set_tuning(const gsph_tuning &t) {
-        if (t.sparse_total < 0 || t.sparse_self < 0 || t.mid_total < 0 ||
-            t.ctas_density_tra < 1 || t.ctas_density_tra > kMaxShape.density_tra ||
-            t.ctas_density_sms < 1 || t.ctas_density_sms > kMaxShape.density_sms ||
-            t.ctas_force_tra < 1 || t.ctas_force_tra > kMaxShape.force_tra ||
-            t.ctas_force_sms < 1 || t.ctas_force_sms > kMaxShape.force_sms) {
-            set_error("gsph_set_tuning: thresholds must be >= 0 and CTAs per SM in "
-                      "[1, %d/%d/%d/%d]", kMaxShape.density_tra, kMaxShape.density_sms,
-                      kMaxShape.force_tra, kMaxShape.force_sms);
+        const int warps = t.warps_per_block == 0 ? kMaxShape.warps : t.warps_per_block;
+        const int k = (warps == kMaxShape.warps / 2) ? 2 : 1;
+        if ((warps != kMaxShape.warps && warps != kMaxShape.warps / 2) ||
+            t.sparse_total < 0 || t.sparse_self < 0 || t.mid_total < 0 ||
+            t.ctas_density_tra < 1 || t.ctas_density_tra > k * kMaxShape.density_tra ||
+            t.ctas_density_sms < 1 || t.ctas_density_sms > k * kMaxShape.density_sms ||
+            t.ctas_force_tra < 1 || t.ctas_force_tra > k * kMaxShape.force_tra ||
+            t.ctas_force_sms < 1 || t.ctas_force_sms > k * kMaxShape.force_sms) {
+            set_error("gsph_set_tuning: thresholds must be >= 0, warps per block %d or %d, "
+                      "and CTAs per SM in [1, %d/%d/%d/%d] (twice that with %d warps)",
+                      kMaxShape.warps, kMaxShape.warps / 2, kMaxShape.density_tra,
+                      kMaxShape.density_sms, kMaxShape.force_tra, kMaxShape.force_sms,
+                      kMaxShape.warps / 2);
             return GSPH_ERR_INVALID_ARG;
         }
         dp.sparse_total = t.sparse_total;
         dp.sparse_self = t.sparse_self;
         dp.mid_total = t.mid_total;
         shape = {t.ctas_density_tra, t.ctas_density_sms, t.ctas_force_tra,
-                 t.ctas_force_sms};
+                 t.ctas_force_sms, warps};
         drop_graphs();   // the captured launches carry the old values
         return GSPH_OK;
     }
@@ -1635,6 +1641,7 @@ gsph_status gsph_tuning_default(gsph_tuning *out) {
     out->ctas_density_sms = kMaxShape.density_sms;
     out->ctas_force_tra = kMaxShape.force_tra;
     out->ctas_force_sms = kMaxShape.force_sms;
+    out->warps_per_block = kMaxShape.warps;
     return GSPH_OK;
 }
 
@@ -1679,24 +1686,36 @@ gsph_status gsph_set_viscosity_model(gsph_handle h, int model, float alpha, floa
 }
 
 // Built-in candidates: four split-threshold sets (the reference's, all TRA,
-// SMS-leaning, TRA-leaning) x two CTA counts for each TRA pass.
+// SMS-leaning, TRA-leaning), each with block shapes of 8 and 4 warps, the
+// largest and a smaller CTA count for each TRA pass, and for the SMS passes
+// (with 8 warps) the largest and a smaller count: 4 x (2 x 2 x 2 + 2) = 40.
 static std::vector<gsph_tuning> default_candidates() {
     std::vector<gsph_tuning> c;
     const int thr[4][3] = {{96, 15, 60}, {0x7FFFFFFF, 0x7FFFFFFF, 60},
                            {48, 8, 30}, {192, 30, 120}};
-    for (const auto &t : thr)
-        for (int dt : {kMaxShape.density_tra, kMaxShape.density_tra - 2})
-            for (int ft : {kMaxShape.force_tra, kMaxShape.force_tra - 1}) {
-                gsph_tuning g{};
-                g.sparse_total = t[0];
-                g.sparse_self = t[1];
-                g.mid_total = t[2];
-                g.ctas_density_tra = dt;
-                g.ctas_density_sms = kMaxShape.density_sms;
-                g.ctas_force_tra = ft;
-                g.ctas_force_sms = kMaxShape.force_sms;
-                c.push_back(g);
-            }
+    auto add = [&](const int *t, int warps, int dt, int ds, int ft, int fs) {
+        gsph_tuning g{};
+        g.sparse_total = t[0];
+        g.sparse_self = t[1];
+        g.mid_total = t[2];
+        g.ctas_density_tra = dt;
+        g.ctas_density_sms = ds;
+        g.ctas_force_tra = ft;
+        g.ctas_force_sms = fs;
+        g.warps_per_block = warps;
+        c.push_back(g);
+    };
+    const LaunchShape m = kMaxShape;
+    for (const auto &t : thr) {
+        for (int w : {m.warps, m.warps / 2}) {
+            const int k = w == m.warps ? 1 : 2;
+            for (int dt : {k * m.density_tra, k * (m.density_tra - 2)})
+                for (int ft : {k * m.force_tra, k * (m.force_tra - 1)})
+                    add(t, w, dt, k * m.density_sms, ft, k * m.force_sms);
+        }
+        add(t, m.warps, m.density_tra, m.density_sms - 1, m.force_tra, m.force_sms - 1);
+        add(t, m.warps, m.density_tra, m.density_sms - 2, m.force_tra, m.force_sms - 2);
+    }
     return c;
 }
 

@@ -150,13 +150,16 @@ typedef struct {
  * (gpu_model.cu:172-180: a cell stays TRA while its 7-cell total is below
  * sparse_total and its own count below sparse_self; below mid_total it gets
  * (n+27)>>5 SMS tasks, else (n+31)>>5) and this library's launch shapes (CTAs
- * per SM of each pass, at most 6 / 6 / 4 / 4). Other thresholds change which
+ * per SM of the TRA density, SMS density, TRA force and SMS force passes, at
+ * most 6 / 4 / 4 / 4 with 8 warps per block, twice that with 4; the blocks of
+ * 4 warps are the same kernels built for that shape). Other thresholds change which
  * cells take the SMS path: results stay within the parity tolerances but the
  * split is no longer the reference's. */
 typedef struct {
     int32_t sparse_total, sparse_self, mid_total;
     int32_t ctas_density_tra, ctas_density_sms, ctas_force_tra, ctas_force_sms;
-    int32_t reserved_;
+    int32_t warps_per_block;   /* 8 (0 reads as 8) or 4; with 4 the CTA counts
+                                * may go up to twice the limits above */
 } gsph_tuning;
 
 /* Fields for gsph_copy_out / gsph_copy_in. All particle fields are in the

@@ -112,3 +112,47 @@ def test_autotune_leaves_the_grid_to_be_rebuilt(gsph, oracle, cuda_device):
     rho, _ = oracle.density(spos, ks, cs, p)
     err = np.abs(1.0 / spos[:, 3].astype(np.float64) - rho) / rho
     assert err.max() <= RHO_TOL
+
+
+@pytest.mark.parametrize("scene", ["sparse", "dense"])
+def test_block_shapes_give_the_same_bits(gsph, cuda_device, scene):
+    """Blocks of 4 warps (the same kernels built for that shape, twice the
+    CTAs per SM) change only the scheduling: every particle's arithmetic and
+    order are the same, so frames are bit-identical to blocks of 8 warps."""
+    if scene == "sparse":
+        _, p, pos = dam_scene(gsph, n_side=18, box=(0.8, 0.5, 0.5))
+    else:
+        _, p, pos = dense_scene(gsph, n_side=20)
+    outs = []
+    for warps, k in ((8, 1), (4, 2), (4, 1)):
+        with gsph.HybridSystem(params=p, positions=shuffled(pos)) as h:
+            t = gsph.tuning_default()
+            t.warps_per_block = warps
+            t.ctas_density_tra *= k
+            t.ctas_density_sms *= k
+            t.ctas_force_tra *= k
+            t.ctas_force_sms *= k
+            h.set_tuning(t)
+            assert h.get_tuning().warps_per_block == warps
+            h.step(4)
+            outs.append(_state(gsph, h))
+    for other in outs[1:]:
+        for x, y in zip(outs[0], other):
+            assert np.array_equal(x, y)
+
+
+def test_block_shape_validation(gsph, cuda_device):
+    _, p, pos = dam_scene(gsph, n_side=6)
+    with gsph.HybridSystem(params=p, positions=pos) as h:
+        for warps, dt in ((6, 6), (4, 13), (8, 7)):
+            t = gsph.tuning_default()
+            t.warps_per_block = warps
+            t.ctas_density_tra = dt
+            with pytest.raises(gsph.GsphError) as ei:
+                h.set_tuning(t)
+            assert ei.value.status == gsph.ERR_INVALID_ARG
+        t = gsph.tuning_default()
+        t.warps_per_block = 4
+        t.ctas_density_tra = 12
+        h.set_tuning(t)
+        h.step(2)
