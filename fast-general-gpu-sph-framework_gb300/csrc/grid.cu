@@ -104,39 +104,19 @@ __device__ __forceinline__ void load_tile_counts(const int32_t *__restrict__ in,
     }
 }
 
-__global__ void __launch_bounds__(kScanThreads)
-k_cell_scan_reduce(const int32_t *__restrict__ count, int numc,
-                   unsigned long long *__restrict__ tiles) {
-    const int first = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
-    int v[kScanItems];
-    load_tile_counts(count, numc, first, v);
-    unsigned long long s = 0;
-#pragma unroll
-    for (int q = 0; q < kScanItems; ++q) s += pack_cell(v[q]);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(kFull, s, o);
-    __shared__ unsigned long long ws[kScanThreads / 32];
-    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        unsigned long long t = 0;
-        for (int w = 0; w < kScanThreads / 32; ++w) t += ws[w];
-        tiles[blockIdx.x] = t;
-    }
-}
-
-// Exclusive scan of the tile sums by one CTA; writes the grand total.
-__global__ void __launch_bounds__(1024)
-k_cell_scan_tiles(unsigned long long *__restrict__ tiles, int ntiles,
-                  int32_t *__restrict__ cell_start, int numc, Counters *ctr) {
+// Exclusive scan of the packed tile sums by one block (any multiple of 32
+// threads), in place; returns the grand total to thread 0. The tiles were
+// written by other CTAs of the same launch, so they are read from L2.
+__device__ unsigned long long scan_tile_sums(unsigned long long *tiles, int ntiles) {
     __shared__ unsigned long long ws[32];
     __shared__ unsigned long long carry;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = int(blockDim.x >> 5);
     for (int base = 0; base < ntiles; base += blockDim.x) {
         const int t = base + threadIdx.x;
-        const unsigned long long v = t < ntiles ? tiles[t] : 0ull;
+        const unsigned long long v = t < ntiles ? __ldcg(tiles + t) : 0ull;
         unsigned long long x = v;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -146,13 +126,13 @@ k_cell_scan_tiles(unsigned long long *__restrict__ tiles, int ntiles,
         if (lane == 31) ws[warp] = x;
         __syncthreads();
         if (warp == 0) {
-            unsigned long long w = ws[lane];
+            unsigned long long w = lane < nw ? ws[lane] : 0ull;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 unsigned long long y = __shfl_up_sync(kFull, w, o);
                 if (lane >= o) w += y;
             }
-            ws[lane] = w;
+            if (lane < nw) ws[lane] = w;
         }
         __syncthreads();
         const unsigned long long wprefix = warp > 0 ? ws[warp - 1] : 0ull;
@@ -162,15 +142,49 @@ k_cell_scan_tiles(unsigned long long *__restrict__ tiles, int ntiles,
         if (threadIdx.x == blockDim.x - 1) carry = excl + v;
         __syncthreads();
     }
+    return carry;
+}
+
+// Tile sums of the packed (occupied, count) values; the last CTA to finish
+// (a counter, no waiting) scans the tile sums, writes the grand total and
+// resets the frame's work counters.
+__global__ void __launch_bounds__(kScanThreads)
+k_cell_scan_reduce(const int32_t *__restrict__ count, int numc,
+                   unsigned long long *__restrict__ tiles, int32_t *__restrict__ cell_start,
+                   Counters *ctr) {
+    const int first = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    int v[kScanItems];
+    load_tile_counts(count, numc, first, v);
+    unsigned long long s = 0;
+#pragma unroll
+    for (int q = 0; q < kScanItems; ++q) s += pack_cell(v[q]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(kFull, s, o);
+    __shared__ unsigned long long ws[kScanThreads / 32];
+    __shared__ bool last;
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
     if (threadIdx.x == 0) {
-        cell_start[numc] = int32_t(carry & 0xFFFFFFFFull);
-        ctr->num_occ = int32_t(carry >> 32);
+        unsigned long long t = 0;
+        for (int w = 0; w < kScanThreads / 32; ++w) t += ws[w];
+        tiles[blockIdx.x] = t;
+        __threadfence();
+        last = atomicAdd(&ctr->scan_done, 1) == int(gridDim.x) - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const unsigned long long total = scan_tile_sums(tiles, int(gridDim.x));
+    if (threadIdx.x == 0) {
+        cell_start[numc] = int32_t(total & 0xFFFFFFFFull);
+        ctr->num_occ = int32_t(total >> 32);
         ctr->num_big = 0;
         ctr->work_density = 0;
         ctr->work_force = 0;
         ctr->work_density_sms = 0;
         ctr->work_force_sms = 0;
         ctr->any_sms = 0;
+        ctr->scan_done = 0;
     }
 }
 
@@ -487,9 +501,7 @@ void launch_hash_count(const Frame &f, const DevParams &P, cudaStream_t s) {
 void launch_cell_scan(const Frame &f, const DevParams &P, cudaStream_t s) {
     const int ntiles = (P.numc + kScanTile - 1) / kScanTile;
     k_cell_scan_reduce<<<ntiles, kScanThreads, 0, s>>>(f.cell_count, P.numc,
-                                                       f.scan_tiles);
-    k_cell_scan_tiles<<<1, 1024, 0, s>>>(f.scan_tiles, ntiles, f.cell_start,
-                                        P.numc, f.ctr);
+                                                       f.scan_tiles, f.cell_start, f.ctr);
     k_cell_scan_apply<<<ntiles, kScanThreads, 0, s>>>(
         f.cell_count, P.numc, f.scan_tiles, f.cell_start, f.occ_list,
         f.big_list, f.ctr);

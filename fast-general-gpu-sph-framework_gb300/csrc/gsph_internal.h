@@ -42,6 +42,9 @@ constexpr int kMaskRowMax = 32;
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanThreads * kScanItems;
+// Tiles of the per-occupied-cell {tasks, SMS, TRA} scan of the split.
+constexpr int kValItems = 4;
+constexpr int kValTile = kScanThreads * kValItems;
 
 // Error bits raised by kernels into Counters::err.
 enum : uint32_t {
@@ -132,7 +135,11 @@ struct Counters {
     // particle is TRA, the compact index is the identity and the TRA/SMS
     // compaction is skipped.
     int32_t any_sms;
-    int32_t pad[20];
+    // CTAs of the cell-count reduction / of the performance model that have
+    // written their tile sums; the last one scans the tiles (and resets it).
+    int32_t scan_done;
+    int32_t model_done;
+    int32_t pad[18];
 };
 
 // Per-frame device pointers of one batch of scenes.

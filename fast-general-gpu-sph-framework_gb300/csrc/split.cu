@@ -31,16 +31,10 @@ __device__ __forceinline__ int cell_n(const int32_t *__restrict__ start, int c) 
 }
 
 // A6: SMS task count of one cell (gpu_model.cu:137-181, same neighbour
-// bounds tests; the thresholds are the reference's unless tuned).
-__global__ void __launch_bounds__(256)
-k_cell_model(const int32_t *__restrict__ occ, Counters *ctr,
-             const int32_t *__restrict__ start, SceneTable T, int3 thr,
-             int4 *__restrict__ val) {
-    const int num_occ = ctr->num_occ;
-    bool any = false;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < num_occ;
-         k += gridDim.x * blockDim.x) {
-    const int gidx = occ[k];
+// bounds tests; the thresholds are the reference's unless tuned), with the
+// cell's SMS and TRA particle counts: {req, sms, tra, 0}.
+__device__ __forceinline__ int4 cell_model(int gidx, const int32_t *__restrict__ start,
+                                           const SceneTable &T, int3 thr) {
     const SceneGeom G = geom_of_cell(T, gidx);
     const int idx = gidx - G.cbase;           // the scene's own cell index
     const int grid_x = G.gx, grid_y = G.gy;
@@ -64,10 +58,7 @@ k_cell_model(const int32_t *__restrict__ occ, Counters *ctr,
     else
         req = (self + 31) >> 5;
     const int sms = min(req * kSmsTaskParticles, self);
-    val[k] = make_int4(req, sms, self - sms, 0);
-    any |= req > 0;
-    }
-    if (__any_sync(kFull, any) && (threadIdx.x & 31) == 0) atomicOr(&ctr->any_sms, 1);
+    return make_int4(req, sms, self - sms, 0);
 }
 
 __device__ __forceinline__ int4 add4(int4 a, int4 b) {
@@ -84,19 +75,76 @@ __device__ __forceinline__ int4 shfl_down4(int4 v, int o) {
                      __shfl_down_sync(kFull, v.w, o));
 }
 
-// Reduce-then-scan of int4 values over a device-side count (num_occ).
+// Exclusive scan, in place, of the int4 tile sums by one block; returns the
+// grand total. The tiles were written by other CTAs of the same launch, so
+// they are read from L2.
+__device__ int4 scan_val_tiles(int4 *tiles, int ntiles) {
+    __shared__ int4 ws[32];
+    __shared__ int4 carry;
+    if (threadIdx.x == 0) carry = make_int4(0, 0, 0, 0);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = int(blockDim.x >> 5);
+    for (int base = 0; base < ntiles; base += blockDim.x) {
+        const int t = base + threadIdx.x;
+        const int4 v = t < ntiles ? __ldcg(tiles + t) : make_int4(0, 0, 0, 0);
+        int4 x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int4 y = shfl_up4(x, o);
+            if (lane >= o) x = add4(x, y);
+        }
+        if (lane == 31) ws[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            int4 w = lane < nw ? ws[lane] : make_int4(0, 0, 0, 0);
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int4 y = shfl_up4(w, o);
+                if (lane >= o) w = add4(w, y);
+            }
+            if (lane < nw) ws[lane] = w;
+        }
+        __syncthreads();
+        const int4 wprefix = warp > 0 ? ws[warp - 1] : make_int4(0, 0, 0, 0);
+        int4 excl = add4(carry, wprefix);
+        excl = make_int4(excl.x + x.x - v.x, excl.y + x.y - v.y, excl.z + x.z - v.z, 0);
+        if (t < ntiles) tiles[t] = excl;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = add4(excl, v);
+        __syncthreads();
+    }
+    return carry;
+}
+
+// A6 + the reduction of A7: the performance model of every occupied cell
+// ({req, sms, tra} per cell, kValTile cells per tile) and each tile's sum.
+// The last CTA to finish (a counter, no waiting) scans the tile sums and
+// sets the task count, the SMS particle count and the middle value; in a
+// frame where no cell takes the SMS path it only records that.
 __global__ void __launch_bounds__(kScanThreads)
-k_val_scan_reduce(const int4 *__restrict__ in, const Counters *ctr,
-                  int4 *__restrict__ tiles) {
-    if (!ctr->any_sms) return;   // all TRA: nothing to compact
+k_cell_model(const int32_t *__restrict__ occ, Counters *ctr,
+             const int32_t *__restrict__ start, SceneTable T, int3 thr,
+             int4 *__restrict__ val, int4 *__restrict__ tiles, int task_capacity,
+             int n_particles) {
     const int n = ctr->num_occ;
     __shared__ int4 ws[kScanThreads / 32];
-    for (int tile = blockIdx.x; tile * kScanTile < n; tile += gridDim.x) {
-        const int first = tile * kScanTile + threadIdx.x * kScanItems;
+    __shared__ bool last;
+    bool any = false;
+    for (int tile = blockIdx.x; tile * kValTile < n; tile += gridDim.x) {
+        const int first = tile * kValTile + threadIdx.x;
         int4 s = make_int4(0, 0, 0, 0);
-#pragma unroll 4
-        for (int q = 0; q < kScanItems; ++q)
-            if (first + q < n) s = add4(s, in[first + q]);
+        // consecutive threads take consecutive cells (coalesced)
+#pragma unroll
+        for (int q = 0; q < kValItems; ++q) {
+            const int k = first + q * kScanThreads;
+            if (k < n) {
+                const int4 v = cell_model(occ[k], start, T, thr);
+                val[k] = v;
+                any |= v.x > 0;
+                s = add4(s, v);
+            }
+        }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) s = add4(s, shfl_down4(s, o));
         if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
@@ -108,64 +156,36 @@ k_val_scan_reduce(const int4 *__restrict__ in, const Counters *ctr,
         }
         __syncthreads();
     }
-}
-
-__global__ void __launch_bounds__(1024)
-k_val_scan_tiles(int4 *__restrict__ tiles, Counters *ctr, int task_capacity,
-                 int n_particles) {
-    if (!ctr->any_sms) {         // all TRA
+    if (__any_sync(kFull, any) && (threadIdx.x & 31) == 0) atomicOr(&ctr->any_sms, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(&ctr->model_done, 1) == int(gridDim.x) - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const bool sms = atomicAdd(&ctr->any_sms, 0) != 0;
+    if (!sms) {   // all TRA: nothing to compact
         if (threadIdx.x == 0) {
             ctr->task_count = 0;
             ctr->n_sms = 0;
             ctr->middle = n_particles;
+            ctr->model_done = 0;
         }
         return;
     }
-    const int ntiles = (ctr->num_occ + kScanTile - 1) / kScanTile;
-    __shared__ int4 ws[32];
-    __shared__ int4 carry;
-    if (threadIdx.x == 0) carry = make_int4(0, 0, 0, 0);
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int base = 0; base < ntiles; base += blockDim.x) {
-        const int t = base + threadIdx.x;
-        const int4 v = t < ntiles ? tiles[t] : make_int4(0, 0, 0, 0);
-        int4 x = v;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            int4 y = shfl_up4(x, o);
-            if (lane >= o) x = add4(x, y);
-        }
-        if (lane == 31) ws[warp] = x;
-        __syncthreads();
-        if (warp == 0) {
-            int4 w = ws[lane];
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                int4 y = shfl_up4(w, o);
-                if (lane >= o) w = add4(w, y);
-            }
-            ws[lane] = w;
-        }
-        __syncthreads();
-        const int4 wprefix = warp > 0 ? ws[warp - 1] : make_int4(0, 0, 0, 0);
-        int4 excl = add4(carry, wprefix);
-        excl = make_int4(excl.x + x.x - v.x, excl.y + x.y - v.y,
-                         excl.z + x.z - v.z, 0);
-        if (t < ntiles) tiles[t] = excl;
-        __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) carry = add4(excl, v);
-        __syncthreads();
-    }
+    const int4 total = scan_val_tiles(tiles, (n + kValTile - 1) / kValTile);
     if (threadIdx.x == 0) {
-        int tasks = carry.x;
+        int tasks = total.x;
         if (tasks + 1 > task_capacity) {   // +1: odd-tail descriptor
             atomicOr(&ctr->err, kErrTaskCapacity);
             tasks = task_capacity - 1;
         }
         ctr->task_count = tasks;
-        ctr->n_sms = carry.y;
-        ctr->middle = carry.z;
+        ctr->n_sms = total.y;
+        ctr->middle = total.z;
+        ctr->model_done = 0;
     }
 }
 
@@ -175,12 +195,12 @@ k_val_scan_apply(const int4 *__restrict__ in, const Counters *ctr,
     if (!ctr->any_sms) return;
     const int n = ctr->num_occ;
     __shared__ int4 ws[kScanThreads / 32];
-    for (int tile = blockIdx.x; tile * kScanTile < n; tile += gridDim.x) {
-    const int first = tile * kScanTile + threadIdx.x * kScanItems;
-    int4 v[kScanItems];
+    for (int tile = blockIdx.x; tile * kValTile < n; tile += gridDim.x) {
+    const int first = tile * kValTile + threadIdx.x * kValItems;
+    int4 v[kValItems];
     int4 s = make_int4(0, 0, 0, 0);
 #pragma unroll
-    for (int q = 0; q < kScanItems; ++q) {
+    for (int q = 0; q < kValItems; ++q) {
         v[q] = (first + q < n) ? in[first + q] : make_int4(0, 0, 0, 0);
         s = add4(s, v[q]);
     }
@@ -197,7 +217,7 @@ k_val_scan_apply(const int4 *__restrict__ in, const Counters *ctr,
     for (int w = 0; w < warp; ++w) run = add4(run, ws[w]);
     run = make_int4(run.x + x.x - s.x, run.y + x.y - s.y, run.z + x.z - s.z, 0);
 #pragma unroll
-    for (int q = 0; q < kScanItems; ++q) {
+    for (int q = 0; q < kValItems; ++q) {
         if (first + q < n) out[first + q] = run;
         run = add4(run, v[q]);
     }
@@ -336,15 +356,12 @@ void launch_split(const Frame &f, const DevParams &P, int max_occ, int num_sms,
     if (f.n <= 0 || max_occ <= 0) return;
     // grid-stride kernels over the device-side counts, sized for the capacity
     // but at most a few CTAs per SM
-    const int cap256 = std::min((max_occ + 255) / 256, num_sms * 8);
     const int cap128 = std::min((max_occ + 127) / 128, num_sms * 16);
-    const int ntiles = std::min((max_occ + kScanTile - 1) / kScanTile, num_sms * 4);
-    k_cell_model<<<cap256, 256, 0, s>>>(
+    const int ntiles = std::min((max_occ + kValTile - 1) / kValTile, num_sms * 8);
+    k_cell_model<<<ntiles, kScanThreads, 0, s>>>(
         f.occ_list, f.ctr, f.cell_start, f.scenes,
-        make_int3(P.sparse_total, P.sparse_self, P.mid_total), f.cell_val);
-    k_val_scan_reduce<<<ntiles, kScanThreads, 0, s>>>(f.cell_val, f.ctr,
-                                                     f.scan_tiles4);
-    k_val_scan_tiles<<<1, 1024, 0, s>>>(f.scan_tiles4, f.ctr, f.task_capacity, f.n);
+        make_int3(P.sparse_total, P.sparse_self, P.mid_total), f.cell_val, f.scan_tiles4,
+        f.task_capacity, f.n);
     k_val_scan_apply<<<ntiles, kScanThreads, 0, s>>>(f.cell_val, f.ctr,
                                                     f.scan_tiles4, f.cell_prefix);
     k_cell_emit<<<cap128, 128, 0, s>>>(

@@ -336,7 +336,7 @@ struct System {
             (st = alloc_n(&fr.nbr_mask, ((N + 31) / 32) * 32 * 9)) ||
             (st = alloc_n(&fr.nbr_flag, N)) ||
             (st = alloc_n(&fr.scan_tiles, (C + kScanTile - 1) / kScanTile)) ||
-            (st = alloc_n(&fr.scan_tiles4, size_t((occ_cap + kScanTile - 1) / kScanTile))) ||
+            (st = alloc_n(&fr.scan_tiles4, size_t((occ_cap + kValTile - 1) / kValTile))) ||
             (st = alloc_n(&fr.ctr, 1)) ||
             (st = alloc_n(&red, size_t(8 + 8 * 512))) ||
             (st = alloc_n(&d_geom, size_t(s_cap))) ||
