@@ -211,7 +211,6 @@ gsph_status gsph_server_step(gsph_server_handle s, int *frames_stepped) {
             bytes += r.bytes();
         }
     }
-    size_t n_admitted = 0;
     {
         std::lock_guard<std::mutex> lock(s->mu);
         for (;;) {
@@ -237,7 +236,6 @@ gsph_status gsph_server_step(gsph_server_handle s, int *frames_stepped) {
                 bytes += h.bytes();
                 pl.admitted.push_back(std::move(s->queue.front()));
                 s->queue.pop_front();
-                ++n_admitted;
             }
             // a head that cannot fit even alone would block the queue forever
             if (!s->queue.empty()) {
@@ -251,7 +249,10 @@ gsph_status gsph_server_step(gsph_server_handle s, int *frames_stepped) {
             break;
         }
     }
-    if (plan.size() > s->shards.size()) s->shards.resize(plan.size());
+    if (plan.size() > s->shards.size()) {
+        std::lock_guard<std::mutex> lock(s->mu);   // get_stats walks the shards
+        s->shards.resize(plan.size());
+    }
     for (size_t b = 0; b < plan.size(); ++b) {
         Shard &sh = s->shards[b];
         ShardPlan &pl = plan[b];
@@ -283,7 +284,6 @@ gsph_status gsph_server_step(gsph_server_handle s, int *frames_stepped) {
         }
         sh.resident = std::move(next);
     }
-    (void)n_admitted;
     // 2. step all resident scenes up to the earliest completion: every batch
     //    is launched on its own stream first, then all are waited for
     uint32_t k = uint32_t(cfg.chunk_frames);
@@ -308,7 +308,7 @@ gsph_status gsph_server_step(gsph_server_handle s, int *frames_stepped) {
             for (Request &r : sh.resident) r.remaining -= k;
     }
     std::vector<Request> done;
-    for (Shard &sh : s->shards) {
+    for (Shard &sh : s->shards) {   // resident lists change only on this thread
         for (size_t i = 0; i < sh.resident.size(); ++i) {
             const Request &r = sh.resident[i];
             if (r.remaining) continue;
