@@ -4,7 +4,10 @@
 // (src/main.cpp:42-85 parseBenchmarkFrames / runHeadlessBenchmark and the print
 // block of HybridSystem::runBenchmark, src/simulation/sph_hybrid_system.cpp:
 // 397-429), plus --scene PATH (the reference compiles the scene path in),
-// --device D and --graph (launch whole frames as CUDA graphs of 10 frames).
+// --device D, --graph (launch whole frames as CUDA graphs of 10 frames),
+// --artificial-viscosity ALPHA C0 (Monaghan's artificial viscosity in place of
+// the reference's Laplacian term) and --autotune (time the built-in tunings
+// on the scene and keep the fastest before the benchmark).
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -54,6 +57,33 @@ int main(int argc, char **argv) {
     gsph_info info;
     gsph_get_info(h, &info);
     std::printf("Number of particles: %u\n", info.n_particles);
+    for (int i = 1; i + 2 < argc; ++i)
+        if (!std::strcmp(argv[i], "--artificial-viscosity")) {
+            st = gsph_set_viscosity_model(h, GSPH_VISCOSITY_ARTIFICIAL,
+                                          float(std::atof(argv[i + 1])),
+                                          float(std::atof(argv[i + 2])));
+            if (st) {
+                std::fprintf(stderr, "%s\n", gsph_last_error());
+                gsph_destroy(h);
+                return EXIT_FAILURE;
+            }
+            std::printf("Artificial viscosity: alpha %s, c0 %s\n", argv[i + 1], argv[i + 2]);
+        }
+    if (has_flag(argc, argv, "--autotune")) {
+        gsph_tuning best;
+        float ms = 0.f;
+        st = gsph_autotune(h, 3, nullptr, 0, &best, &ms);
+        if (st) {
+            std::fprintf(stderr, "%s\n", gsph_last_error());
+            gsph_destroy(h);
+            return EXIT_FAILURE;
+        }
+        std::printf("Autotuned: thresholds %d/%d/%d, CTAs per SM %d/%d/%d/%d, %d warps per "
+                    "block (%.4f ms per trial frame)\n",
+                    best.sparse_total, best.sparse_self, best.mid_total, best.ctas_density_tra,
+                    best.ctas_density_sms, best.ctas_force_tra, best.ctas_force_sms,
+                    best.warps_per_block, double(ms));
+    }
     // --graph: whole frames launched as CUDA graphs of 10 frames
     if (has_flag(argc, argv, "--graph")) gsph_set_graph_mode(h, 10);
     gsph_bench_report r;

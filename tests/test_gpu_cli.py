@@ -55,3 +55,18 @@ def test_bad_arguments_fail_cleanly(gsph, cuda_device, tmp_path):
     assert rc != 0 and "positive" in err
     rc, out, err = _run(gsph, ["--benchmark", "3", "--scene", str(tmp_path / "missing.json")])
     assert rc != 0 and err.strip()
+
+
+def test_cli_artificial_viscosity_and_autotune(gsph, cuda_device, tmp_path):
+    scene = tmp_path / "scene.json"
+    scene.write_text(dam_scene_text(n_side=12, seed=2))
+    rc, out, err = _run(gsph, ["--benchmark", "6", "--scene", str(scene),
+                               "--artificial-viscosity", "0.02", "20", "--autotune", "--graph"])
+    assert rc == 0, err
+    assert "Artificial viscosity: alpha 0.02, c0 20" in out
+    assert re.search(r"Autotuned: thresholds \d+/\d+/\d+, CTAs per SM \d+/\d+/\d+/\d+, "
+                     r"[48] warps per block", out)
+    assert "FPS:" in out
+    rc, out, err = _run(gsph, ["--benchmark", "3", "--scene", str(scene),
+                               "--artificial-viscosity", "0", "20"])
+    assert rc != 0 and "alpha and c0" in err
