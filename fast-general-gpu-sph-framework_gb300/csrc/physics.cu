@@ -41,10 +41,21 @@ __device__ __forceinline__ float powf_7(float b) {
 }
 
 // Squared distance with one fixed rounding sequence (x^2, then + y^2, then
-// + z^2, each fused), shared by every pass so that the density pass's
-// neighbour masks and the force pass's cut-off test agree bit for bit.
+// + z^2, each fused), shared by the force passes and the SMS density pass.
 __device__ __forceinline__ float sq_dist(float dx, float dy, float dz) {
     return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+// The TRA density pass's cut-off test in one unsigned compare: with
+// e = d^2 - kFloatSmall (the subtraction folded into the first fused
+// multiply-add), the reference's kFloatSmall <= d^2 <= h^2 is
+// 0 <= e <= h^2 - kFloatSmall, and for FP32 values that is
+// bits(e) <= bits(h^2 - kFloatSmall) (a negative e has its sign bit set).
+// The weight (h^2 - d^2) is then (h^2 - kFloatSmall) - e. Only roundings
+// differ from the two-compare form; pairs at the cut-off contribute zero
+// either way.
+__device__ __forceinline__ float sq_dist_less_small(float dx, float dy, float dz) {
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, -kFloatSmall)));
 }
 
 // Start of micro-x slab `lo` of cell c (0 = cell start).
@@ -341,6 +352,8 @@ k_density_tra(Frame f, DevParams P) {
         int incomplete = 0;
         int found = 0;
         float sum = 0.f;
+        const float cut = P.h2 - kFloatSmall;
+        const uint32_t cut_bits = __float_as_uint(cut);
         for (int r = 0; r < 9; ++r) {
             const int ny = mp.cy + (r % 3) - 1;
             const int nz = mp.cz + (r / 3) - 1;
@@ -355,9 +368,9 @@ k_density_tra(Frame f, DevParams P) {
                 for (int j = begin; j < end; ++j, bit <<= 1) {
                     const float4 q = f.pos[j];
                     const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
-                    const float d2 = sq_dist(dx, dy, dz);
-                    if (P.h2 < d2 || kFloatSmall > d2) continue;
-                    const float t = P.h2 - d2;
+                    const float e = sq_dist_less_small(dx, dy, dz);
+                    if (__float_as_uint(e) > cut_bits) continue;
+                    const float t = cut - e;
                     sum += t * t * t;
                     mask |= bit;
                 }
