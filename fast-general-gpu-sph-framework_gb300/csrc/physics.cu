@@ -41,7 +41,7 @@ __device__ __forceinline__ float powf_7(float b) {
 }
 
 // Squared distance with one fixed rounding sequence (x^2, then + y^2, then
-// + z^2, each fused), shared by the force passes and the SMS density pass.
+// + z^2, each fused), shared by the force passes.
 __device__ __forceinline__ float sq_dist(float dx, float dy, float dz) {
     return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
 }
@@ -497,8 +497,8 @@ __device__ __forceinline__ void task_z_range(const Frame &f, int self, bool acti
 // One 32-particle task per warp (density_kernels.cu:368-565). Candidates are
 // streamed 256 at a time into shared memory, each pair (slots 2k, 2k+1) as an
 // (x, x, y, y) float4 and a (z, z) float2; every lane evaluates them two at a
-// time with packed FP32x2 arithmetic (distances and h^2 - r^2 round exactly
-// as the scalar form).
+// time with packed FP32x2 arithmetic and the TRA pass's one-compare cut-off
+// test.
 template <int W>
 __global__ void __launch_bounds__(W * 32, 4 * kWarpsPerBlock / W)
 k_density_sms(Frame f, DevParams P) {
@@ -529,7 +529,10 @@ k_density_sms(Frame f, DevParams P) {
         const float2 npx = make_float2(-p.x, -p.x);
         const float2 npy = make_float2(-p.y, -p.y);
         const float2 npz = make_float2(-p.z, -p.z);
-        const float2 h2v = make_float2(P.h2, P.h2);
+        const float cut = P.h2 - kFloatSmall;
+        const uint32_t cut_bits = __float_as_uint(cut);
+        const float2 cutv = make_float2(cut, cut);
+        const float2 msm = make_float2(-kFloatSmall, -kFloatSmall);
         const float2 m1 = make_float2(-1.f, -1.f);
         float2 acc = make_float2(0.f, 0.f);
         sms_stream(
@@ -554,12 +557,13 @@ k_density_sms(Frame f, DevParams P) {
                     const float2 dx = __fadd2_rn(make_float2(qa.x, qa.y), npx);
                     const float2 dy = __fadd2_rn(make_float2(qa.z, qa.w), npy);
                     const float2 dz = __fadd2_rn(szz[k], npz);
-                    float2 d2 = __fmul2_rn(dx, dx);
-                    d2 = __ffma2_rn(dy, dy, d2);
-                    d2 = __ffma2_rn(dz, dz, d2);
-                    float2 t = __ffma2_rn(d2, m1, h2v);
-                    t.x = (t.x < 0.f || d2.x < kFloatSmall) ? 0.f : t.x;
-                    t.y = (t.y < 0.f || d2.y < kFloatSmall) ? 0.f : t.y;
+                    // the cut-off test of sq_dist_less_small, per half
+                    float2 e = __ffma2_rn(dx, dx, msm);
+                    e = __ffma2_rn(dy, dy, e);
+                    e = __ffma2_rn(dz, dz, e);
+                    float2 t = __ffma2_rn(e, m1, cutv);
+                    t.x = __float_as_uint(e.x) > cut_bits ? 0.f : t.x;
+                    t.y = __float_as_uint(e.y) > cut_bits ? 0.f : t.y;
                     acc = __ffma2_rn(__fmul2_rn(t, t), t, acc);
                 }
             });
