@@ -253,8 +253,11 @@ void launch_cell_scan(const Frame &f, const DevParams &P, cudaStream_t s);
 void launch_scatter_pairs(const Frame &f, cudaStream_t s);
 void launch_cell_sort(const Frame &f, int num_sms, cudaStream_t s);
 // ---- launchers (split.cu) ----
+// Performance model, TRA/SMS partition and SMS tasks; launch_judge then
+// pairs the tasks (judgeTask), which only the SMS passes read.
 void launch_split(const Frame &f, const DevParams &P, int max_occ, int num_sms,
                   cudaStream_t s);
+void launch_judge(const Frame &f, int max_occ, int num_sms, cudaStream_t s);
 // ---- launchers (physics.cu) ----
 // Launch shapes of the density and force passes: CTAs per SM of each kernel.
 struct LaunchShape {
@@ -266,12 +269,14 @@ constexpr LaunchShape kMaxShape = {6, 4, 4, 4, 8};   // the kernels' launch boun
 // Shared-memory carveouts of the density and force kernels (once per
 // device, before their first launch).
 cudaError_t configure_physics_kernels(int device);
+// The TRA pass on s, the SMS pass on s_sms (the two touch disjoint particles
+// and work counters; the caller joins them before the results are read).
 void launch_density(const Frame &f, const DevParams &P, int num_sms,
-                    const LaunchShape &shape, cudaStream_t s);
+                    const LaunchShape &shape, cudaStream_t s, cudaStream_t s_sms);
 // fresh: the density pass ran on the current state, so the TRA neighbour
 // masks are valid.
 void launch_force(const Frame &f, const DevParams &P, int num_sms, bool fresh,
-                  const LaunchShape &shape, cudaStream_t s);
+                  const LaunchShape &shape, cudaStream_t s, cudaStream_t s_sms);
 void launch_integrate(const Frame &f, const DevParams &P, cudaStream_t s);
 // Render-side buffers (headless): packed RGBA colour per particle from its
 // density and its path (TRA, paired SMS, single SMS), and render-space

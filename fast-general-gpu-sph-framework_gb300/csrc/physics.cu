@@ -1022,16 +1022,16 @@ cudaError_t configure_shape(int smem) {
 
 template <int W>
 void launch_density_w(const Frame &f, const DevParams &P, int num_sms,
-                      const LaunchShape &shape, cudaStream_t s) {
+                      const LaunchShape &shape, cudaStream_t s, cudaStream_t s_sms) {
+    k_density_sms<W><<<num_sms * shape.density_sms, W * 32, 0, s_sms>>>(f, P);
     k_density_tra<W><<<num_sms * shape.density_tra, W * 32, 0, s>>>(f, P);
-    k_density_sms<W><<<num_sms * shape.density_sms, W * 32, 0, s>>>(f, P);
 }
 
 template <bool kArt, int W>
 void launch_force_w(const Frame &f, const DevParams &P, int num_sms, bool fresh,
-                    const LaunchShape &shape, cudaStream_t s) {
+                    const LaunchShape &shape, cudaStream_t s, cudaStream_t s_sms) {
+    k_force_sms<kArt, W><<<num_sms * shape.force_sms, W * 32, 0, s_sms>>>(f, P);
     k_force_tra<kArt, W><<<num_sms * shape.force_tra, W * 32, 0, s>>>(f, P, fresh);
-    k_force_sms<kArt, W><<<num_sms * shape.force_sms, W * 32, 0, s>>>(f, P);
 }
 
 }  // namespace
@@ -1046,28 +1046,28 @@ cudaError_t configure_physics_kernels(int device) {
 }
 
 void launch_density(const Frame &f, const DevParams &P, int num_sms,
-                    const LaunchShape &shape, cudaStream_t s) {
+                    const LaunchShape &shape, cudaStream_t s, cudaStream_t s_sms) {
     if (f.n <= 0) return;
     if (shape.warps == kWarpsPerBlock / 2)
-        launch_density_w<kWarpsPerBlock / 2>(f, P, num_sms, shape, s);
+        launch_density_w<kWarpsPerBlock / 2>(f, P, num_sms, shape, s, s_sms);
     else
-        launch_density_w<kWarpsPerBlock>(f, P, num_sms, shape, s);
+        launch_density_w<kWarpsPerBlock>(f, P, num_sms, shape, s, s_sms);
 }
 
 void launch_force(const Frame &f, const DevParams &P, int num_sms, bool fresh,
-                  const LaunchShape &shape, cudaStream_t s) {
+                  const LaunchShape &shape, cudaStream_t s, cudaStream_t s_sms) {
     if (f.n <= 0) return;
     const bool half = shape.warps == kWarpsPerBlock / 2;
     if (P.visc_artificial) {
         if (half)
-            launch_force_w<true, kWarpsPerBlock / 2>(f, P, num_sms, fresh, shape, s);
+            launch_force_w<true, kWarpsPerBlock / 2>(f, P, num_sms, fresh, shape, s, s_sms);
         else
-            launch_force_w<true, kWarpsPerBlock>(f, P, num_sms, fresh, shape, s);
+            launch_force_w<true, kWarpsPerBlock>(f, P, num_sms, fresh, shape, s, s_sms);
     } else {
         if (half)
-            launch_force_w<false, kWarpsPerBlock / 2>(f, P, num_sms, fresh, shape, s);
+            launch_force_w<false, kWarpsPerBlock / 2>(f, P, num_sms, fresh, shape, s, s_sms);
         else
-            launch_force_w<false, kWarpsPerBlock>(f, P, num_sms, fresh, shape, s);
+            launch_force_w<false, kWarpsPerBlock>(f, P, num_sms, fresh, shape, s, s_sms);
     }
 }
 

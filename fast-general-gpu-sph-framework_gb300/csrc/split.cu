@@ -367,6 +367,10 @@ void launch_split(const Frame &f, const DevParams &P, int max_occ, int num_sms,
     k_cell_emit<<<cap128, 128, 0, s>>>(
         f.occ_list, f.ctr, f.cell_start, f.key, f.cell_val, f.cell_prefix,
         f.scenes, f.compact, f.tasks);
+}
+
+void launch_judge(const Frame &f, int max_occ, int num_sms, cudaStream_t s) {
+    if (f.n <= 0 || max_occ <= 0) return;   // as launch_split: no tasks made
     const int max_pairs = (f.task_capacity + 1) / 2;
     k_judge<<<std::min((max_pairs + 127) / 128, num_sms * 8), 128, 0, s>>>(f.tasks,
                                                                           f.ctr);

@@ -138,6 +138,23 @@ struct System {
     }
     std::vector<std::vector<cudaEvent_t>> ev_pending;   // 5 events per frame
 
+    // The SMS side of the density and force stages (task pairing, SMS
+    // density, SMS force) runs on a second stream beside the TRA passes:
+    // fork() orders it after the main stream's work so far, join() orders
+    // the main stream after it. Inside a capture the pair becomes a fork
+    // and a join of the graph. In an all-TRA frame the SMS launches, which
+    // find no work, then cost the frame nothing.
+    cudaStream_t aux = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    void fork() {
+        cudaEventRecord(fork_ev, stream);
+        cudaStreamWaitEvent(aux, fork_ev, 0);
+    }
+    void join() {
+        cudaEventRecord(join_ev, aux);
+        cudaStreamWaitEvent(stream, join_ev, 0);
+    }
+
     ~System() { release(); }
 
     void release() {
@@ -166,6 +183,16 @@ struct System {
             cudaEventDestroy(frames_done);
             frames_done = nullptr;
         }
+        if (aux) {
+            cudaStreamSynchronize(aux);
+            cudaStreamDestroy(aux);
+            aux = nullptr;
+        }
+        for (cudaEvent_t *e : {&fork_ev, &join_ev})
+            if (*e) {
+                cudaEventDestroy(*e);
+                *e = nullptr;
+            }
         xfer_pending = false;
         for (void *p : allocs) cudaFree(p);
         allocs.clear();
@@ -299,6 +326,9 @@ struct System {
         num_sms = device_sm_count(device);
         GSPH_CUDA(configure_physics_kernels(device));
         GSPH_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        GSPH_CUDA(cudaStreamCreateWithFlags(&aux, cudaStreamNonBlocking));
+        GSPH_CUDA(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+        GSPH_CUDA(cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming));
         long long n_total = 0, c_total = 0;
         if (count < 1) {
             set_error("a batch needs at least one scene at creation");
@@ -507,7 +537,9 @@ struct System {
         sms_pending = false;
     }
 
-    void enqueue_arrange(int in) {
+    // pair_tasks: also pair the SMS tasks (judgeTask) here; a frame leaves
+    // that to its density stage, on the second stream.
+    void enqueue_arrange(int in, bool pair_tasks = true) {
         lists_valid = false;
         const Frame f = frame_arrange(in);
         if (!hashed)
@@ -518,16 +550,24 @@ struct System {
         launch_scatter_pairs(f, stream);
         launch_cell_sort(f, num_sms, stream);
         launch_split(f, dp, max_occ, num_sms, stream);
+        if (pair_tasks) launch_judge(f, max_occ, num_sms, stream);
         hashed = false;          // consumed; the sort cleared the counts
         sms_pending = false;
         counts_dirty = false;
     }
-    void enqueue_density(int b) {
-        launch_density(frame_physics(b), dp, num_sms, shape, stream);
+    // pair_tasks: the arrange left the task pairing to this stage.
+    void enqueue_density(int b, bool pair_tasks = false) {
+        const Frame f = frame_physics(b);
+        fork();
+        if (pair_tasks) launch_judge(f, max_occ, num_sms, aux);
+        launch_density(f, dp, num_sms, shape, stream, aux);
+        join();
         lists_valid = true;
     }
     void enqueue_force(int b) {
-        launch_force(frame_physics(b), dp, num_sms, lists_valid, shape, stream);
+        fork();
+        launch_force(frame_physics(b), dp, num_sms, lists_valid, shape, stream, aux);
+        join();
     }
     // Force on buffer b with the integration fused in: the new state goes to
     // buffer 1 - b (the previous frame's unsorted copy, no longer read), in
@@ -540,7 +580,9 @@ struct System {
         f.vel_next = vel[1 - b];
         f.ev_next = ev[1 - b];
         f.hash_next = true;
-        launch_force(f, dp, num_sms, lists_valid, shape, stream);
+        fork();
+        launch_force(f, dp, num_sms, lists_valid, shape, stream, aux);
+        join();
         lists_valid = false;
         hashed = true;
         sms_pending = true;
@@ -580,8 +622,8 @@ struct System {
         hashed = true;
         sms_pending = false;
         for (int k = 0; k < graph_frames; ++k) {
-            enqueue_arrange(parity);
-            enqueue_density(1 - parity);
+            enqueue_arrange(parity, false);
+            enqueue_density(1 - parity, true);
             enqueue_force_advance(1 - parity, k == graph_frames - 1);
         }
         cudaError_t e = cudaStreamEndCapture(stream, &g);
@@ -621,9 +663,9 @@ struct System {
             for (int k = 0; k < 5; ++k) evs.push_back(take_event());
             cudaEventRecord(evs[0], stream);
         }
-        enqueue_arrange(in);
+        enqueue_arrange(in, false);
         if (timing) cudaEventRecord(evs[1], stream);
-        enqueue_density(out);
+        enqueue_density(out, true);
         if (timing) cudaEventRecord(evs[2], stream);
         enqueue_force_advance(out, keep_acc);
         if (timing) {
