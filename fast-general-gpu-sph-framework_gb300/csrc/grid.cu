@@ -297,9 +297,17 @@ __global__ void __launch_bounds__(256) k_sort_small(Frame f) {
     const int b = f.cell_start[cell];
     const int cnt = f.cell_start[cell + 1] - b;
     if (cnt > kSmallCellMax) return;
+    // the particle's state is gathered while its rank is computed
+    const int src = int(e & 0xFFFFFFFFull);
+    const float4 pos = f.pos_in[src], vel = f.vel_in[src], ev = f.ev_in[src];
     int rank = 0;
     for (int j = 0; j < cnt; ++j) rank += (f.pairs[b + j] < e) ? 1 : 0;
-    move_particle(f, b + rank, e);
+    const int dst = b + rank;
+    f.key[dst] = uint32_t(e >> 32);
+    f.perm[dst] = src;
+    f.pos[dst] = pos;
+    f.vel[dst] = vel;
+    f.ev[dst] = ev;
     if (rank == 0) {
         // group counts, 8 bits each (cnt <= 32), packed in two words
         unsigned long long lo = 0, hi = 0;
