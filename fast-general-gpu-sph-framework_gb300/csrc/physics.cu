@@ -600,18 +600,26 @@ k_force_tra(Frame f, DevParams P, bool fresh) {
         ForceAcc a = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         const int found = fresh ? f.nbr_flag[idx] : -1;
         if (found >= 0) {
+            // all nine masks, then every row's offsets and slab word, loaded
+            // without conditions (a row without neighbours reads the
+            // particle's own cell) so that the loads are in flight together
             const uint32_t *masks = f.nbr_mask + size_t(u) * 9 * 32 + lane;
+            uint32_t mk[9];
+#pragma unroll
+            for (int r = 0; r < 9; ++r) mk[r] = masks[r * 32];
+            const int own = G.cbase + mp.cx + G.gx * (mp.cy + G.gy * mp.cz);
+            const int left = mp.cx > 0 ? 1 : 0;
+#pragma unroll
             for (int r = 0; r < 9; ++r) {
-                const uint32_t mask = masks[r * 32];
-                row_mask[r][threadIdx.x] = mask;
-                if (mask) {
-                    const int ny = mp.cy + (r % 3) - 1;
-                    const int nz = mp.cz + (r / 3) - 1;
-                    const int m = G.cbase + mp.cx + G.gx * (ny + G.gy * nz);
-                    row_start[r][threadIdx.x] = mp.cx > 0
-                        ? slab_begin(f, m - 1, f.cell_start[m - 1], f.cell_start[m], mp.lmx)
-                        : f.cell_start[m];
-                }
+                const int m = mk[r] ? own + G.gx * ((r % 3) - 1 + G.gy * ((r / 3) - 1)) : own;
+                const int s0 = f.cell_start[m - left];
+                const int s1 = f.cell_start[m];
+                const uint32_t xs = f.cell_xslab[m - left];
+                int start = s0;
+                if (left && mp.lmx > 0 && xs != kXslabUnknown)
+                    start = s0 + min(int((xs >> (10 * (mp.lmx - 1))) & 1023u), s1 - s0);
+                row_mask[r][threadIdx.x] = mk[r];
+                row_start[r][threadIdx.x] = start;
             }
             int r = 0;
             uint32_t mask = row_mask[0][threadIdx.x];
