@@ -311,6 +311,10 @@ __device__ __forceinline__ void write_force(const Frame &f, const DevParams &P,
     }
 }
 
+// Cell-array bytes past which the TRA density pass prefetches its rows'
+// offsets: about half of the GB300's L2.
+constexpr size_t kRowPrefetchCellBytes = size_t(64) << 20;
+
 // Warps per block of the density and force kernels: 8 by default; each
 // kernel is also built for 4 (gsph_tuning.warps_per_block), with twice the
 // CTAs per SM for the same occupancy.
@@ -332,7 +336,13 @@ __device__ __forceinline__ int next_unit(int *counter) {
 // One particle per lane, 32 consecutive TRA particles per work unit
 // (density_kernels.cu:318-366). Which candidates of each row interact is also
 // recorded as a bit mask for the force pass.
-template <int W>
+//
+// kRowPrefetch: each lane first prefetches its nine rows' cell offsets and
+// slab words into L1, so that the per-row set-up inside the row loop waits on
+// L1 rather than DRAM. Chosen on the host when the cell arrays are too large
+// to stay in L2 (large batches); otherwise the extra instructions cost more
+// than they save.
+template <int W, bool kRowPrefetch>
 __global__ void __launch_bounds__(W * 32, 6 * kWarpsPerBlock / W)
 k_density_tra(Frame f, DevParams P) {
     const int lane = threadIdx.x & 31;
@@ -354,6 +364,19 @@ k_density_tra(Frame f, DevParams P) {
         float sum = 0.f;
         const float cut = P.h2 - kFloatSmall;
         const uint32_t cut_bits = __float_as_uint(cut);
+        if (kRowPrefetch) {
+            const int left = mp.cx > 0 ? 1 : 0;
+#pragma unroll
+            for (int r = 0; r < 9; ++r) {
+                const int ny = mp.cy + (r % 3) - 1;
+                const int nz = mp.cz + (r / 3) - 1;
+                if (ny >= 0 && ny < G.gy && nz >= 0 && nz < G.gz) {
+                    const int m = G.cbase + mp.cx - left + G.gx * (ny + G.gy * nz);
+                    asm volatile("prefetch.global.L1 [%0];" :: "l"(f.cell_start + m));
+                    asm volatile("prefetch.global.L1 [%0];" :: "l"(f.cell_xslab + m));
+                }
+            }
+        }
         for (int r = 0; r < 9; ++r) {
             const int ny = mp.cy + (r % 3) - 1;
             const int nz = mp.cz + (r / 3) - 1;
@@ -1015,7 +1038,9 @@ template <int W>
 cudaError_t configure_shape(int smem) {
     const int k = kWarpsPerBlock / W;   // CTAs per SM scale with the block size
     cudaError_t e;
-    if ((e = set_carveout(k_density_tra<W>, kMaxShape.density_tra * k, smem, W * 32)))
+    if ((e = set_carveout(k_density_tra<W, false>, kMaxShape.density_tra * k, smem, W * 32)))
+        return e;
+    if ((e = set_carveout(k_density_tra<W, true>, kMaxShape.density_tra * k, smem, W * 32)))
         return e;
     if ((e = set_carveout(k_density_sms<W>, kMaxShape.density_sms * k, smem, W * 32)))
         return e;
@@ -1030,9 +1055,13 @@ cudaError_t configure_shape(int smem) {
 
 template <int W>
 void launch_density_w(const Frame &f, const DevParams &P, int num_sms,
-                      const LaunchShape &shape, cudaStream_t s, cudaStream_t s_sms) {
+                      const LaunchShape &shape, cudaStream_t s, cudaStream_t s_sms,
+                      bool row_prefetch) {
     k_density_sms<W><<<num_sms * shape.density_sms, W * 32, 0, s_sms>>>(f, P);
-    k_density_tra<W><<<num_sms * shape.density_tra, W * 32, 0, s>>>(f, P);
+    if (row_prefetch)
+        k_density_tra<W, true><<<num_sms * shape.density_tra, W * 32, 0, s>>>(f, P);
+    else
+        k_density_tra<W, false><<<num_sms * shape.density_tra, W * 32, 0, s>>>(f, P);
 }
 
 template <bool kArt, int W>
@@ -1056,10 +1085,12 @@ cudaError_t configure_physics_kernels(int device) {
 void launch_density(const Frame &f, const DevParams &P, int num_sms,
                     const LaunchShape &shape, cudaStream_t s, cudaStream_t s_sms) {
     if (f.n <= 0) return;
+    // cell offsets and slab words: 8 bytes per cell
+    const bool row_prefetch = size_t(P.numc) * 8 > kRowPrefetchCellBytes;
     if (shape.warps == kWarpsPerBlock / 2)
-        launch_density_w<kWarpsPerBlock / 2>(f, P, num_sms, shape, s, s_sms);
+        launch_density_w<kWarpsPerBlock / 2>(f, P, num_sms, shape, s, s_sms, row_prefetch);
     else
-        launch_density_w<kWarpsPerBlock>(f, P, num_sms, shape, s, s_sms);
+        launch_density_w<kWarpsPerBlock>(f, P, num_sms, shape, s, s_sms, row_prefetch);
 }
 
 void launch_force(const Frame &f, const DevParams &P, int num_sms, bool fresh,
