@@ -245,11 +245,18 @@ k_scatter_pairs(const uint32_t *__restrict__ key_in,
                 const uint32_t *__restrict__ slot, int n,
                 const int32_t *__restrict__ cell_start,
                 unsigned long long *__restrict__ pairs) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t key = key_in[i];
-    const int dst = cell_start[key >> 6] + int(slot[i]);
-    pairs[dst] = ((unsigned long long)key << 32) | (unsigned)i;
+    // two particles per thread, a block-width apart: both chains of loads
+    // are in flight together
+    const int i0 = blockIdx.x * (2 * blockDim.x) + threadIdx.x;
+    const int i1 = i0 + blockDim.x;
+    uint32_t k0 = 0, k1 = 0, s0 = 0, s1 = 0;
+    if (i0 < n) { k0 = key_in[i0]; s0 = slot[i0]; }
+    if (i1 < n) { k1 = key_in[i1]; s1 = slot[i1]; }
+    int c0 = 0, c1 = 0;
+    if (i0 < n) c0 = cell_start[k0 >> 6];
+    if (i1 < n) c1 = cell_start[k1 >> 6];
+    if (i0 < n) pairs[c0 + int(s0)] = ((unsigned long long)k0 << 32) | (unsigned)i0;
+    if (i1 < n) pairs[c1 + int(s1)] = ((unsigned long long)k1 << 32) | (unsigned)i1;
 }
 
 __device__ __forceinline__ uint32_t pack_xslab(int s1, int s2, int s3, int cnt) {
@@ -287,45 +294,79 @@ __device__ __forceinline__ void move_particle(const Frame &f, int dst,
     f.ev[dst] = f.ev_in[src];
 }
 
-// Cells with at most kSmallCellMax particles: one thread per particle ranks
-// its pair among the cell's pairs (all distinct: sources are unique).
-__global__ void __launch_bounds__(256) k_sort_small(Frame f) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= f.n) return;
-    const unsigned long long e = f.pairs[s];
-    const uint32_t cell = uint32_t(e >> 38);
-    const int b = f.cell_start[cell];
-    const int cnt = f.cell_start[cell + 1] - b;
-    if (cnt > kSmallCellMax) return;
-    // the particle's state is gathered while its rank is computed
-    const int src = int(e & 0xFFFFFFFFull);
-    const float4 pos = f.pos_in[src], vel = f.vel_in[src], ev = f.ev_in[src];
-    int rank = 0;
-    for (int j = 0; j < cnt; ++j) rank += (f.pairs[b + j] < e) ? 1 : 0;
-    const int dst = b + rank;
-    f.key[dst] = uint32_t(e >> 32);
-    f.perm[dst] = src;
-    f.pos[dst] = pos;
-    f.vel[dst] = vel;
-    f.ev[dst] = ev;
-    if (rank == 0) {
-        // group counts, 8 bits each (cnt <= 32), packed in two words
-        unsigned long long lo = 0, hi = 0;
-        for (int j = 0; j < cnt; ++j) {
-            const int g = int((f.pairs[b + j] >> 34) & 15ull);
-            if (g < 8)
-                lo += 1ull << (8 * g);
-            else
-                hi += 1ull << (8 * (g - 8));
-        }
-        int n16[16];
+// Group offsets and slab words of a small cell, written by the thread of the
+// cell's first particle, which also clears the cell's count.
+__device__ __forceinline__ void small_cell_groups(const Frame &f, uint32_t cell, int b,
+                                                  int cnt) {
+    // group counts, 8 bits each (cnt <= 32), packed in two words
+    unsigned long long lo = 0, hi = 0;
+    for (int j = 0; j < cnt; ++j) {
+        const int g = int((f.pairs[b + j] >> 34) & 15ull);
+        if (g < 8)
+            lo += 1ull << (8 * g);
+        else
+            hi += 1ull << (8 * (g - 8));
+    }
+    int n16[16];
 #pragma unroll
-        for (int g = 0; g < 8; ++g) {
-            n16[g] = int((lo >> (8 * g)) & 0xFF);
-            n16[g + 8] = int((hi >> (8 * g)) & 0xFF);
+    for (int g = 0; g < 8; ++g) {
+        n16[g] = int((lo >> (8 * g)) & 0xFF);
+        n16[g + 8] = int((hi >> (8 * g)) & 0xFF);
+    }
+    write_groups(f, cell, n16, cnt);
+    f.cell_count[cell] = 0;   // ready for the next frame's atomics
+}
+
+// Cells with at most kSmallCellMax particles: one thread per particle ranks
+// its pair among the cell's pairs (all distinct: sources are unique). Each
+// thread takes two particles a block-width apart and issues both particles'
+// loads (pair, cell bounds, state, the cell's pairs) before any store, so
+// that the two chains of loads are in flight together.
+__global__ void __launch_bounds__(256) k_sort_small(Frame f) {
+    int s[2];
+    s[0] = blockIdx.x * (2 * blockDim.x) + threadIdx.x;
+    s[1] = s[0] + blockDim.x;
+    unsigned long long e[2] = {0ull, 0ull};
+    int b[2] = {0, 0}, cnt[2] = {0, 0}, rank[2] = {0, 0};
+    bool live[2];
+    float4 pos[2], vel[2], ev[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        live[k] = s[k] < f.n;
+        if (live[k]) e[k] = f.pairs[s[k]];
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        if (live[k]) {
+            const uint32_t cell = uint32_t(e[k] >> 38);
+            b[k] = f.cell_start[cell];
+            cnt[k] = f.cell_start[cell + 1] - b[k];
+            live[k] = cnt[k] <= kSmallCellMax;
         }
-        write_groups(f, cell, n16, cnt);
-        f.cell_count[cell] = 0;   // ready for the next frame's atomics
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        if (live[k]) {
+            const int src = int(e[k] & 0xFFFFFFFFull);
+            pos[k] = f.pos_in[src];
+            vel[k] = f.vel_in[src];
+            ev[k] = f.ev_in[src];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+        if (live[k])
+            for (int j = 0; j < cnt[k]; ++j) rank[k] += (f.pairs[b[k] + j] < e[k]) ? 1 : 0;
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        if (!live[k]) continue;
+        const int dst = b[k] + rank[k];
+        f.key[dst] = uint32_t(e[k] >> 32);
+        f.perm[dst] = int(e[k] & 0xFFFFFFFFull);
+        f.pos[dst] = pos[k];
+        f.vel[dst] = vel[k];
+        f.ev[dst] = ev[k];
+        if (rank[k] == 0) small_cell_groups(f, uint32_t(e[k] >> 38), b[k], cnt[k]);
     }
 }
 
@@ -517,13 +558,13 @@ void launch_cell_scan(const Frame &f, const DevParams &P, cudaStream_t s) {
 
 void launch_scatter_pairs(const Frame &f, cudaStream_t s) {
     if (f.n <= 0) return;
-    k_scatter_pairs<<<(f.n + 255) / 256, 256, 0, s>>>(f.key_in, f.slot, f.n,
+    k_scatter_pairs<<<(f.n + 511) / 512, 256, 0, s>>>(f.key_in, f.slot, f.n,
                                                      f.cell_start, f.pairs);
 }
 
 void launch_cell_sort(const Frame &f, int num_sms, cudaStream_t s) {
     if (f.n <= 0) return;
-    k_sort_small<<<(f.n + 255) / 256, 256, 0, s>>>(f);
+    k_sort_small<<<(f.n + 511) / 512, 256, 0, s>>>(f);
     k_sort_big<<<num_sms * 4, 256, 0, s>>>(f);
 }
 
