@@ -49,7 +49,7 @@ SCENE = "dam_break_3_94m.json"
 WORKLOAD = ("dam_break_3_94m: 158^3 = 3,944,312 FP32 particles, dx 0.01 m, h 0.02 m, "
             "jitter +-0.05dx, box 4.74x3.16x1.68 m (237x159x84 cells), Tait B=57142.857, "
             "viscosity 0.8, dt 1e-4 s")
-LAUNCHES_PER_FRAME = 14   # hash of SMS particles + 5 grid sort + 4 split + 2 density + 2 force
+LAUNCHES_PER_FRAME = 14   # 5 grid sort + 4 split + 2 density + 2 force + SMS hash
 
 
 def dist_env():

@@ -50,8 +50,9 @@ k_hash_count(const float4 *__restrict__ pos, int n, DevParams P, SceneTable T,
     slot_out[i] = cell_slot(cell_count, key >> 6, active);
 }
 
-// The particles the previous split sent to SMS tasks (compact[middle, n)),
-// whose keys the force pass did not compute ahead.
+// The particles the split sent to SMS tasks (compact[middle, n)), hashed
+// ahead from their integrated positions after the SMS force pass (the TRA
+// force pass hashes its own particles).
 __global__ void __launch_bounds__(256)
 k_hash_sms(const float4 *__restrict__ pos, int n, DevParams P, SceneTable T,
            const int32_t *__restrict__ compact, uint32_t *__restrict__ key_out,
@@ -534,10 +535,11 @@ __global__ void __launch_bounds__(256) k_sort_big(Frame f) {
 
 }  // namespace
 
-void launch_hash_sms(const Frame &f, const DevParams &P, cudaStream_t s) {
+void launch_hash_sms(const Frame &f, const float4 *pos, const DevParams &P,
+                     cudaStream_t s) {
     if (f.n <= 0) return;
     k_hash_sms<<<std::min((f.n + 255) / 256, 4096), 256, 0, s>>>(
-        f.pos_in, f.n, P, f.scenes, f.compact, f.key_in, f.slot, f.cell_count, f.ctr);
+        pos, f.n, P, f.scenes, f.compact, f.key_in, f.slot, f.cell_count, f.ctr);
 }
 
 void launch_hash_count(const Frame &f, const DevParams &P, cudaStream_t s) {

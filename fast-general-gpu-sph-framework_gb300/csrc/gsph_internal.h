@@ -154,8 +154,8 @@ struct Frame {
     float4 *pos_next, *vel_next, *ev_next;
     // With pos_next set and hash_next true, the TRA force pass also computes
     // the next frame's micro key and cell slot of its particles (key_in, slot,
-    // cell_count); the SMS particles are hashed at the start of the next
-    // arrange (launch_hash_sms), before the split overwrites the compact list.
+    // cell_count); launch_hash_sms does the same for the SMS particles after
+    // the SMS force pass.
     bool hash_next;
     uint32_t *key_in, *slot;                   // per source particle
     unsigned long long *pairs;                 // (key << 32 | src), by cell
@@ -248,7 +248,10 @@ __device__ __forceinline__ uint32_t cell_slot(int32_t *cell_count, uint32_t cell
 // ---- launchers (grid.cu) ----
 void launch_hash_count(const Frame &f, const DevParams &P, cudaStream_t s);
 // Hash of the previous split's SMS particles only (compact[middle, n)).
-void launch_hash_sms(const Frame &f, const DevParams &P, cudaStream_t s);
+// Keys and cell slots ahead for the split's SMS particles (compact[middle,
+// n)) from their integrated positions `pos`.
+void launch_hash_sms(const Frame &f, const float4 *pos, const DevParams &P,
+                     cudaStream_t s);
 void launch_cell_scan(const Frame &f, const DevParams &P, cudaStream_t s);
 void launch_scatter_pairs(const Frame &f, cudaStream_t s);
 void launch_cell_sort(const Frame &f, int num_sms, cudaStream_t s);

@@ -303,7 +303,7 @@ __device__ __forceinline__ void write_force(const Frame &f, const DevParams &P,
         f.pos_next[self] = po;
         f.vel_next[self] = vo;
         f.ev_next[self] = eo;
-        if (f.hash_next && !sms) {   // SMS particles: k_hash_sms next frame
+        if (f.hash_next && !sms) {   // SMS particles: launch_hash_sms
             const uint32_t key = micro_key(po, P, G, f.ctr, self);
             f.key_in[self] = key;
             f.slot[self] = cell_slot(f.cell_count, key >> 6, __activemask());

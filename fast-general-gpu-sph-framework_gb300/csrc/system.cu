@@ -106,9 +106,6 @@ struct System {
     // hold counts that no arrange will consume (cleared before a new hash).
     bool hashed = false;
     bool counts_dirty = false;
-    // sms_pending: the hash ahead covered the TRA particles only; the previous
-    // split's SMS particles still need theirs (launch_hash_sms).
-    bool sms_pending = false;
     uint64_t frames = 0;
 
     LaunchShape shape = kMaxShape;   // CTAs per SM of the density/force kernels
@@ -528,13 +525,7 @@ struct System {
             cudaMemsetAsync(fr.cell_count, 0, sizeof(int32_t) * size_t(c_cap), stream);
         launch_hash_count(frame_arrange(in), dp, stream);
         hashed = true;
-        sms_pending = false;
         counts_dirty = true;
-    }
-    // Completes a TRA-only hash ahead with the previous split's SMS particles.
-    void enqueue_hash_sms(int in) {
-        launch_hash_sms(frame_arrange(in), dp, stream);
-        sms_pending = false;
     }
 
     // pair_tasks: also pair the SMS tasks (judgeTask) here; a frame leaves
@@ -542,17 +533,13 @@ struct System {
     void enqueue_arrange(int in, bool pair_tasks = true) {
         lists_valid = false;
         const Frame f = frame_arrange(in);
-        if (!hashed)
-            enqueue_hash(in);
-        else if (sms_pending)
-            enqueue_hash_sms(in);
+        if (!hashed) enqueue_hash(in);
         launch_cell_scan(f, dp, stream);
         launch_scatter_pairs(f, stream);
         launch_cell_sort(f, num_sms, stream);
         launch_split(f, dp, max_occ, num_sms, stream);
         if (pair_tasks) launch_judge(f, max_occ, num_sms, stream);
         hashed = false;          // consumed; the sort cleared the counts
-        sms_pending = false;
         counts_dirty = false;
     }
     // pair_tasks: the arrange left the task pairing to this stage.
@@ -582,10 +569,12 @@ struct System {
         f.hash_next = true;
         fork();
         launch_force(f, dp, num_sms, lists_valid, shape, stream, aux);
+        // the SMS particles' keys ahead, after their force pass on the
+        // second stream (beside the TRA force pass, which hashes its own)
+        launch_hash_sms(f, f.pos_next, dp, aux);
         join();
         lists_valid = false;
         hashed = true;
-        sms_pending = true;
         counts_dirty = true;
     }
     void enqueue_advance(int b) {
@@ -620,7 +609,6 @@ struct System {
         GSPH_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         // graph launches are preceded by a complete hash of the state
         hashed = true;
-        sms_pending = false;
         for (int k = 0; k < graph_frames; ++k) {
             enqueue_arrange(parity, false);
             enqueue_density(1 - parity, true);
@@ -688,7 +676,6 @@ struct System {
         if (graph_frames > 0 && !timing) {
             // captured frames start from a hashed state and leave one behind
             if (n >= graph_frames && !hashed) enqueue_hash(cur);
-            if (n >= graph_frames && sms_pending) enqueue_hash_sms(cur);
             GSPH_CUDA(cudaGetLastError());
             while (n >= graph_frames) {
                 if (!graph[cur]) {
@@ -698,8 +685,6 @@ struct System {
                 GSPH_CUDA(cudaGraphLaunch(graph[cur], stream));
                 hashed = true;
                 counts_dirty = true;
-                if (n - graph_frames >= graph_frames) enqueue_hash_sms(cur);
-                else sms_pending = true;
                 arranged = true;
                 grid_current = false;
                 lists_valid = false;

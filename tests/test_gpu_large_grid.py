@@ -8,7 +8,8 @@ The fluid is the same block of particles in a 0.8 x 0.5 x 0.5 m box
 candidates are visited in the same order in both (rows in a fixed (dy, dz)
 order, each row left to right along x, each cell in micro-key order), so
 density and force must agree bit for bit, particle by particle; both must be
-within the parity bounds of the FP64 oracle.
+within the parity bounds of the FP64 oracle. The large box runs with blocks of
+8 and of 4 warps (both builds of the prefetching pass).
 """
 import numpy as np
 import pytest
@@ -22,8 +23,12 @@ FORCE_TOL = 1e-4
 FORCE_SUM_TOL = 64 * 2.0 ** -24
 
 
-def _frame(gsph, p, pos, vel):
+def _frame(gsph, p, pos, vel, warps=8):
     with gsph.HybridSystem(params=p, positions=pos, velocities=vel) as h:
+        if warps != 8:
+            t = gsph.tuning_default()
+            t.warps_per_block = warps
+            h.set_tuning(t)
         h.arrange()
         h.copy_in(gsph.FIELD_EVAL_VELOCITY, h.copy_out(gsph.FIELD_VELOCITY))
         h.density()
@@ -38,7 +43,8 @@ def _frame(gsph, p, pos, vel):
     return out, info
 
 
-def test_large_grid_matches_small_box_and_fp64(gsph, oracle, cuda_device):
+@pytest.mark.parametrize("warps", [8, 4])
+def test_large_grid_matches_small_box_and_fp64(gsph, oracle, cuda_device, warps):
     _, p_small, pos = dam_scene(gsph, n_side=24, box=(0.8, 0.5, 0.5))
     _, p_large, pos_l = dam_scene(gsph, n_side=24, box=(5.12, 5.12, 3.2))
     assert np.array_equal(pos, pos_l)
@@ -50,7 +56,7 @@ def test_large_grid_matches_small_box_and_fp64(gsph, oracle, cuda_device):
     vel = np.zeros_like(pos)
     vel[:, :3] = rng.normal(0.0, 0.3, (len(pos), 3))
     small, info_s = _frame(gsph, p_small, pos, vel)
-    large, info_l = _frame(gsph, p_large, pos, vel)
+    large, info_l = _frame(gsph, p_large, pos, vel, warps)
     assert info_s.tra_particles == len(pos) and info_l.tra_particles == len(pos)
 
     # per source particle: same bits
