@@ -32,8 +32,6 @@ namespace {
 
 constexpr unsigned kFull = 0xFFFFFFFFu;
 
-
-
 // ---------------------------------------------------------------------------
 // A2: key + per-coarse-cell slot (warp-aggregated atomics).
 __global__ void __launch_bounds__(256)
