@@ -339,7 +339,9 @@ gsph_status gsph_advance(gsph_handle h);
 gsph_status gsph_set_graph_mode(gsph_handle h, int frames);
 gsph_status gsph_sync(gsph_handle h);
 /* The handle's CUDA stream (a cudaStream_t), for callers that order their own
- * work or timing events against the handle's kernels. */
+ * work or timing events against the handle's kernels. Some kernels of a frame
+ * run on a second, internal stream, which every call joins back into this one
+ * before it returns, so work ordered after this stream sees all of them. */
 gsph_status gsph_stream(gsph_handle h, void **stream_out);
 
 gsph_status gsph_get_info(gsph_handle h, gsph_info *out);
