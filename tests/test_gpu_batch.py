@@ -70,6 +70,61 @@ def test_dense_batch_bit_identical_to_alone(gsph, cuda_device):
         assert _same(got, _alone(gsph, p, pos, steps))
 
 
+def _alone_model(gsph, p, pos, steps, model):
+    with gsph.HybridSystem(params=p, positions=pos) as s:
+        s.set_viscosity_model(*model)
+        s.step(steps)
+        return [s.copy_out(f) for f in (gsph.FIELD_POSITION, gsph.FIELD_VELOCITY,
+                                        gsph.FIELD_EVAL_VELOCITY, gsph.FIELD_KEY)]
+
+
+def test_artificial_viscosity_batch_bit_identical_to_alone(gsph, cuda_device):
+    """The optional Monaghan viscosity is a handle setting that the batch's
+    force passes read like every other parameter: sparse scenes and a crowded
+    one (TRA and SMS cells) in a batch evolve as each does alone, launched
+    frame by frame and as CUDA graphs."""
+    model = (gsph.VISCOSITY_ARTIFICIAL, 0.02, 20.0)
+    scenes = []
+    for k, (n_side, box) in enumerate([(10, (0.6, 0.4, 0.4)), (14, (0.8, 0.5, 0.5)),
+                                       (8, (0.4, 0.4, 0.4))]):
+        _, p, pos = dam_scene(gsph, n_side=n_side, box=box, seed=20 + k)
+        scenes.append((p, shuffled(pos, seed=k)))
+    crowd = scenes[1][1].copy()
+    crowd[:, :3] = 0.1 + (crowd[:, :3] - 0.1) * 0.4
+    scenes.append((scenes[1][0], crowd))
+    steps = 6
+    for graph in (False, True):
+        with gsph.Batch(scenes) as b:
+            b.set_viscosity_model(*model)
+            b.set_graph_mode(3 if graph else 0)
+            b.step(steps)
+            got = [[b.copy_out_scene(k, f) for f in (gsph.FIELD_POSITION, gsph.FIELD_VELOCITY,
+                                                     gsph.FIELD_EVAL_VELOCITY, gsph.FIELD_KEY)]
+                   for k in range(len(scenes))]
+            info = b.info()
+        assert info.sms_tasks > 0 and info.tra_particles > 0
+        for (p, pos), g in zip(scenes, got):
+            assert _same(g, _alone_model(gsph, p, pos, steps, model))
+
+
+def test_batch_past_the_row_prefetch_size_bit_identical_to_alone(gsph, cuda_device):
+    """Four scenes in 2.25M-cell boxes: together their cell arrays (8 bytes a
+    cell) pass 64 MB, so the batch's TRA density pass is the build that
+    prefetches its rows' offsets, while each scene alone (18 MB) runs the
+    other build. The bits must not change."""
+    scenes = []
+    for k, n_side in enumerate([10, 12, 8, 11]):
+        _, p, pos = dam_scene(gsph, n_side=n_side, box=(3.0, 3.0, 2.0), seed=40 + k)
+        scenes.append((p, shuffled(pos, seed=k)))
+    cells = int(np.prod(list(scenes[0][0].grid_size)))
+    assert cells * 8 < 64 << 20 < 4 * cells * 8
+    steps = 5
+    batched, info = _batch(gsph, scenes, steps)
+    assert info.n_cells == 4 * cells
+    for (p, pos), got in zip(scenes, batched):
+        assert _same(got, _alone(gsph, p, pos, steps))
+
+
 def test_batch_rejects_mixed_physics(gsph, cuda_device):
     _, p1, pos1 = dam_scene(gsph, n_side=6)
     _, p2, pos2 = dense_scene(gsph, n_side=6)
